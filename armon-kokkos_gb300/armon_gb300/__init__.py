@@ -1,0 +1,266 @@
+"""Python access to libarmon_gb300.so (the GB300 Armon time step) through its C ABI.
+
+This module is a thin ctypes layer over include/armon_gb300.h and include/armon_kernels.h: the
+solver, the parameter block and the reference's kernel entry points.  All the compute runs in the
+CUDA library; if the library is missing, importing the bindings raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libarmon_gb300.so")
+
+TESTS = {"Sod": 0, "Sod_y": 1, "Sod_circ": 2, "Bizarrium": 3, "Sedov": 4}
+SCHEMES = {"Godunov": 0, "GAD": 1}
+PROJECTIONS = {"none": 0, "euler": 1, "euler_2nd": 2}
+LIMITERS = {"None": 0, "Minmod": 1, "Superbee": 2}
+SPLITTINGS = {"Sequential": 0, "SequentialSym": 1, "Strang": 2, "X_only": 3, "Y_only": 4}
+ARRAYS = ["x", "y", "rho", "umat", "vmat", "Emat", "pmat", "cmat", "gmat", "ustar", "pstar",
+          "work_array_1", "work_array_2", "work_array_3", "work_array_4", "domain_mask"]
+
+OK, ERR_INVALID_DT, ERR_PARAMS, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM, ERR_STATE = range(7)
+
+
+class ArmonError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"armon error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """armon_params (include/armon_gb300.h): the reference's Params fields."""
+    _fields_ = [(n, C.c_int32) for n in (
+        "test", "scheme", "riemann", "projection", "limiter", "current_axis", "axis_splitting",
+        "nb_ghosts", "nx", "ny", "stencil_width", "cst_dt", "dt_on_even_cycles",
+        "row_length", "col_length", "nb_cells", "ideb", "ifin", "index_start", "idx_row", "idx_col", "s",
+        "cycle", "max_cycles",
+        "write_output", "write_ghosts", "write_throughput", "output_precision", "verbose", "compare")] + [
+        ("dx", C.c_double), ("cfl", C.c_double), ("Dt", C.c_double),
+        ("domain_size", C.c_double * 2), ("domain_origin", C.c_double * 2),
+        ("cycle_dt", C.c_double), ("current_cycle_dt", C.c_double), ("next_cycle_dt", C.c_double),
+        ("time", C.c_double), ("max_time", C.c_double), ("comparison_tolerance", C.c_double),
+        ("test_option", C.c_double)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("seg_len", C.c_int32),
+                ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class Range(C.Structure):
+    _fields_ = [("start", C.c_int64), ("end", C.c_int64)]
+
+
+class InnerRange1D(C.Structure):
+    _fields_ = [("start", C.c_int64), ("step", C.c_int64)]
+
+
+class InnerRange2D(C.Structure):
+    _fields_ = [("main_range_start", C.c_int64), ("main_range_step", C.c_int64),
+                ("row_range_start", C.c_int64), ("row_range_length", C.c_uint64)]
+
+
+class View(C.Structure):
+    """armon_view: a device array of doubles with an optional label."""
+    _fields_ = [("data", C.c_void_p), ("size", C.c_int64), ("label", C.c_char_p)]
+
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with armon-kokkos_gb300/build.py "
+                          "(there is no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    P, S = C.POINTER(Params), C.c_void_p
+    L.armon_last_error.restype = C.c_char_p
+    L.armon_params_defaults.argtypes = [P]
+    L.armon_params_init.argtypes = [P]
+    L.armon_params_check.argtypes = [P]
+    L.armon_min_ghosts.argtypes = [P]
+    L.armon_solver_opts_default.argtypes = [C.POINTER(SolverOpts)]
+    L.armon_solver_create.argtypes = [P, C.POINTER(SolverOpts), C.c_void_p, C.POINTER(C.c_void_p)]
+    L.armon_solver_destroy.argtypes = [S]
+    L.armon_solver_destroy.restype = None
+    for fn in ("armon_solver_init_test", "armon_solver_begin_loop"):
+        getattr(L, fn).argtypes = [S]
+    L.armon_solver_run.argtypes = [S, C.c_int]
+    L.armon_solver_enqueue_cycles.argtypes = [S, C.c_int]
+    L.armon_solver_sync_params.argtypes = [S, P, C.POINTER(C.c_int32)]
+    L.armon_solver_download.argtypes = [S, C.c_int, C.c_void_p]
+    L.armon_solver_upload.argtypes = [S, C.c_int, C.c_void_p]
+    L.armon_solver_device_array.argtypes = [S, C.c_int]
+    L.armon_solver_device_array.restype = C.c_void_p
+    L.armon_solver_conservation.argtypes = [S, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.armon_solver_kernel_launches.argtypes = [S]
+    L.armon_solver_kernel_launches.restype = C.c_int64
+    L.armon_solve_host.argtypes = [P, C.POINTER(SolverOpts), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), P]
+    L.dt_CFL.restype = C.c_double
+    L.idx_size.restype = C.c_int
+    L.is_uidx_signed.restype = C.c_bool
+    L.flt_size.restype = C.c_int
+    L.armon_kernels_set_stream.argtypes = [C.c_void_p]
+    L.armon_kernels_set_stream.restype = None
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise ArmonError(rc, lib().armon_last_error().decode())
+
+
+@dataclass
+class Case:
+    """A configuration in the reference's CLI vocabulary (src/main_2D.cpp:9-38)."""
+    test: str = "Sod"
+    scheme: str = "GAD"
+    projection: str = "euler"
+    limiter: str = "Minmod"
+    splitting: str = "Sequential"
+    nghost: int = 3
+    nx: int = 10
+    ny: int = 10
+    stencil: int = -1
+    cfl: float = 0.0
+    dt: float = 0.0
+    cst_dt: int = 0
+    dt_on_even_cycles: int = 0
+    max_cycles: int = 100
+    max_time: float = 0.0
+    test_option: float = 0.0
+
+
+def make_params(case: Case) -> Params:
+    L = lib()
+    p = Params()
+    L.armon_params_defaults(C.byref(p))
+    p.test = TESTS[case.test]
+    p.scheme = SCHEMES[case.scheme]
+    p.projection = PROJECTIONS[case.projection]
+    p.limiter = LIMITERS[case.limiter]
+    p.axis_splitting = SPLITTINGS[case.splitting]
+    p.nb_ghosts, p.nx, p.ny = case.nghost, case.nx, case.ny
+    p.stencil_width = case.stencil
+    p.cfl, p.Dt = case.cfl, case.dt
+    p.cst_dt, p.dt_on_even_cycles = case.cst_dt, case.dt_on_even_cycles
+    p.max_cycles, p.max_time = case.max_cycles, case.max_time
+    p.test_option = case.test_option
+    L.armon_params_init(C.byref(p))
+    return p
+
+
+class Solver:
+    """A domain resident in HBM with the fused time loop (armon_solver_* of include/armon_gb300.h)."""
+
+    def __init__(self, params: Params | Case, precision: int = 64, stream: int | None = None,
+                 cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 1):
+        L = lib()
+        self.params = make_params(params) if isinstance(params, Case) else params
+        o = SolverOpts()
+        L.armon_solver_opts_default(C.byref(o))
+        o.precision = precision
+        o.cycles_per_graph = cycles_per_graph
+        o.seg_len = seg_len
+        o.block_lines = block_lines
+        o.materialize_eos = materialize_eos
+        self.opts = o
+        h = C.c_void_p()
+        check(L.armon_solver_create(C.byref(self.params), C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().armon_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_test(self) -> None:
+        check(lib().armon_solver_init_test(self._h))
+
+    def begin_loop(self) -> None:
+        check(lib().armon_solver_begin_loop(self._h))
+
+    def run(self, cycle_limit: int = 0) -> None:
+        check(lib().armon_solver_run(self._h, cycle_limit))
+
+    def enqueue_cycles(self, n: int) -> None:
+        check(lib().armon_solver_enqueue_cycles(self._h, n))
+
+    def state(self) -> tuple[Params, int]:
+        p = Params()
+        st = C.c_int32()
+        check(lib().armon_solver_sync_params(self._h, C.byref(p), C.byref(st)))
+        return p, st.value
+
+    def download(self, name: str) -> np.ndarray:
+        a = np.empty(self.params.nb_cells, dtype=np.float64)
+        check(lib().armon_solver_download(self._h, ARRAYS.index(name), a.ctypes.data))
+        return a
+
+    def upload(self, name: str, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == self.params.nb_cells
+        check(lib().armon_solver_upload(self._h, ARRAYS.index(name), a.ctypes.data))
+
+    def device_array(self, name: str) -> int:
+        return lib().armon_solver_device_array(self._h, ARRAYS.index(name)) or 0
+
+    def conservation(self) -> tuple[float, float]:
+        m, e = C.c_double(), C.c_double()
+        check(lib().armon_solver_conservation(self._h, C.byref(m), C.byref(e)))
+        return m.value, e.value
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().armon_solver_kernel_launches(self._h))
+
+
+def real_cells(p: Params, a: np.ndarray) -> np.ndarray:
+    """(ny, nx) view of the real cells of a flat array in the reference's layout."""
+    g, R = p.nb_ghosts, p.row_length
+    return a.reshape(p.col_length, R)[g:g + p.ny, g:g + p.nx]
+
+
+def solve_host(case: Case | Params, inputs: dict[str, np.ndarray] | None = None, precision: int = 64,
+               cycles_per_graph: int = 16) -> tuple[Params, dict[str, np.ndarray]]:
+    """armon_solve_host: the end-to-end call with host buffers (H2D, time loop, D2H)."""
+    L = lib()
+    p = make_params(case) if isinstance(case, Case) else case
+    o = SolverOpts()
+    L.armon_solver_opts_default(C.byref(o))
+    o.precision = precision
+    o.cycles_per_graph = cycles_per_graph
+    ins = (C.c_void_p * 4)()
+    keep = []
+    if inputs:
+        for k, name in enumerate(("rho", "umat", "vmat", "Emat")):
+            if name in inputs:
+                a = np.ascontiguousarray(inputs[name], dtype=np.float64)
+                keep.append(a)
+                ins[k] = a.ctypes.data
+    outs = {name: np.empty(p.nb_cells, dtype=np.float64) for name in ("rho", "umat", "vmat", "Emat", "pmat")}
+    outp = (C.c_void_p * 5)(*[outs[n].ctypes.data for n in ("rho", "umat", "vmat", "Emat", "pmat")])
+    final = Params()
+    check(L.armon_solve_host(C.byref(p), C.byref(o), ins if inputs else None, outp, C.byref(final)))
+    return final, outs

@@ -1,0 +1,122 @@
+// device_common.cuh -- types and device helpers shared by the fused sweep and the stage kernels.
+//
+// Everything here keeps the reference's floating-point semantics exactly: the translation units
+// that include it are compiled with --fmad=false (no contraction) and IEEE division and square
+// root, and min / max are the std::min / std::max ternaries that Kokkos::min / Kokkos::max use
+// (they differ from fmin / fmax on NaN and signed zeros).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace armon {
+
+template <class T> __host__ __device__ __forceinline__ T kmin(T a, T b) { return (b < a) ? b : a; }
+template <class T> __host__ __device__ __forceinline__ T kmax(T a, T b) { return (a < b) ? b : a; }
+
+// Constants of one solve, read by every pass (src/parameters.h:34-108 subset).
+struct StepConfig {
+    double cfl, Dt, max_time;
+    double dt_dx, dt_dy;            // domain_size[0] / nx and domain_size[1] / ny, as dt_CFL uses
+    int32_t cst_dt, dt_on_even_cycles, max_cycles, splitting;
+};
+
+// Device-resident loop state.  Only the last pass of a cycle (or the init kernel) writes it, so
+// every pass of a cycle sees the same values.  raw_dt is dt_CFL of the current state
+// (src/kernels/reductions.cpp:8-24), computed in the epilogue of the pass that produced it.
+struct StepState {
+    double time, current_dt, next_dt, raw_dt;
+    int32_t cycle, status;
+    uint32_t counter;               // block-completion counter of the dt reduction
+    int32_t buf_base;               // state buffer set = (cycle * passes + pass + buf_base) % 2
+};
+
+enum : int32_t { STATUS_RUNNING = 0, STATUS_INVALID_DT = 1 };
+
+// The dt logic of time_step / local_time_step (src/armon_2D.cpp:212-252), evaluated by every
+// pass of a cycle from the committed state.
+struct CycleDt {
+    double current, next;
+    bool run, invalid;
+};
+
+__host__ __device__ inline bool is_finite_d(double x) { return x - x == 0.0; }
+
+__host__ __device__ inline CycleDt cycle_time_step(const StepState& st, const StepConfig& cfg)
+{
+    CycleDt r;
+    r.run = st.status == STATUS_RUNNING && st.time < cfg.max_time && st.cycle < cfg.max_cycles;
+    r.invalid = false;
+    double cur = st.next_dt, nxt;
+    if (cfg.cst_dt) {
+        nxt = cfg.Dt;
+    } else if (!cfg.dt_on_even_cycles || (st.cycle % 2 == 0) || cur == 0) {
+        double dt = st.raw_dt, local;
+        if (!is_finite_d(dt) || dt <= 0)
+            local = dt;
+        else if (cur == 0)
+            local = cfg.cfl * dt;
+        else {
+            double a = cfg.cfl * dt, b = 1.05 * cur;
+            local = (b < a) ? b : a;   // std::min
+        }
+        if (!is_finite_d(local) || local <= 0) r.invalid = true;
+        nxt = local;
+    } else {
+        nxt = cur;
+    }
+    if (st.cycle == 0) cur = nxt;
+    r.current = cur;
+    r.next = nxt;
+    return r;
+}
+
+// Params::split_axes (src/parameters.cpp:212-255) for pass k of `cycle`.
+__host__ __device__ inline void split_axis(int32_t splitting, int32_t cycle, int k, int* axis, double* factor)
+{
+    int a1 = (cycle % 2 == 0) ? 1 : 0;   // Y on even cycles, X on odd
+    int a2 = 1 - a1;
+    *factor = 1.0;
+    switch (splitting) {
+    case 0: *axis = k == 0 ? 0 : 1; break;                                   // Sequential
+    case 1: *axis = k == 0 ? a1 : a2; break;                                 // SequentialSym
+    case 2: *axis = k == 1 ? a2 : a1; *factor = k == 1 ? 1.0 : 0.5; break;   // Strang
+    case 3: *axis = 0; break;                                                // X_only
+    default: *axis = 1; break;                                               // Y_only
+    }
+}
+
+__host__ __device__ inline int passes_per_cycle(int32_t splitting)
+{
+    return splitting == 2 ? 3 : (splitting >= 3 ? 1 : 2);
+}
+
+// The reduction of dt_CFL over the real cells, kept as the two maxima it depends on:
+// min_i RN(dx / a_i) == RN(dx / max_i a_i) for a_i >= 0 because correctly rounded division is
+// monotone, so the per-cell divisions of the reference collapse into one.  A cell whose x term is
+// NaN is skipped whole, and a NaN y term alone is skipped, exactly as the reference's
+// Kokkos::min chain (kmin(acc, kmin(dx/ax, dy/ay)), identity DBL_MAX) treats them.
+struct DtAcc {
+    double ax, ay;
+    __device__ __forceinline__ void init() { ax = 0.0; ay = 0.0; }
+    __device__ __forceinline__ void add(double u, double v, double c)
+    {
+        double mx = kmax(fabs(u + c), fabs(u - c));
+        double my = kmax(fabs(v + c), fabs(v - c));
+        if (mx == mx) {
+            ax = kmax(ax, mx);
+            if (my == my) ay = kmax(ay, my);
+        }
+    }
+    __device__ __forceinline__ void merge(double ox, double oy) { ax = kmax(ax, ox); ay = kmax(ay, oy); }
+};
+
+__host__ __device__ inline double dt_from_maxima(double ax, double ay, double dx, double dy)
+{
+    double qx = dx / ax, qy = dy / ay;
+    double v = kmin(qx, qy);
+    const double dbl_max = 1.7976931348623157e308;
+    return kmin(dbl_max, v);
+}
+
+}  // namespace armon

@@ -1,0 +1,65 @@
+// launch.h -- host-side launchers of the solver kernels, one overload per storage type.
+// sweep_f64.cu (built with --fmad=false: bit-exact FP64) and sweep_f32.cu (FP32 with FMA
+// contraction) define them; solver.cu drives them.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "init.cuh"
+#include "sweep.cuh"
+
+namespace armon {
+
+// Fused axis pass (sweep.cuh).
+cudaError_t launch_sweep(const SweepArgs<double>& a, int scheme, int proj, bool last, int grid, int block,
+                         cudaStream_t st);
+cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
+                         cudaStream_t st);
+
+// init_test over all nb_cells cells (src/kernels/init_test.cpp:51-104).
+struct InitPtrs {
+    void *x, *y, *rho, *Emat, *umat, *vmat, *mask, *pmat, *cmat, *gmat, *ustar, *pstar;
+};
+cudaError_t launch_init_f64(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st);
+cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st);
+inline cudaError_t launch_init(const InitArgs& a, int64_t ncells, const InitPtrs& p, bool fp32, cudaStream_t st)
+{
+    return fp32 ? launch_init_f32(a, ncells, p, st) : launch_init_f64(a, ncells, p, st);
+}
+
+// EOS of the real cells + dt_CFL of that state + reset of the loop state (the start of time_loop,
+// src/armon_2D.cpp:327-346).
+struct BeginArgs {
+    int32_t nx, ny;
+    int64_t origin, row_length;
+    double gamma;
+    void *rho, *umat, *vmat, *Emat, *pmat, *cmat, *gmat;
+    StepState* state;
+    StepConfig cfg;
+    double* partials;
+    int32_t buf_base;
+};
+cudaError_t launch_begin_f64(const BeginArgs& a, int grid, cudaStream_t st);
+cudaError_t launch_begin_f32(const BeginArgs& a, int grid, cudaStream_t st);
+inline cudaError_t launch_begin(const BeginArgs& a, bool fp32, int grid, cudaStream_t st)
+{
+    return fp32 ? launch_begin_f32(a, grid, st) : launch_begin_f64(a, grid, st);
+}
+
+// Sums of rho*ds and rho*ds*E over the real cells in FP64, in a fixed order (two kernels).
+struct ConsArgs {
+    int32_t nx, ny;
+    int64_t origin, row_length;
+    double ds;
+    const void *rho, *Emat;
+    double* partials;   // 2 per block of the first kernel
+    double* out;        // 2 values
+};
+cudaError_t launch_conservation_f64(const ConsArgs& a, int grid, cudaStream_t st);
+cudaError_t launch_conservation_f32(const ConsArgs& a, int grid, cudaStream_t st);
+inline cudaError_t launch_conservation(const ConsArgs& a, bool fp32, int grid, cudaStream_t st)
+{
+    return fp32 ? launch_conservation_f32(a, grid, st) : launch_conservation_f64(a, grid, st);
+}
+
+}  // namespace armon

@@ -1,0 +1,530 @@
+// solver.cu -- the native solver: device-resident state, the fused time loop and its C ABI
+// (include/armon_gb300.h).
+//
+// One cycle = passes_per_cycle(splitting) launches of the fused sweep; the last one also reduces
+// dt_CFL of the new state and commits the cycle (time, cycle, dts) into the device StepState, so
+// the host never waits inside the loop.  Cycles are issued in batches captured in a CUDA graph;
+// after each batch the host reads the 48-byte state back to test the reference's loop condition
+// (time < max_time && cycle < max_cycles).  Cycles issued past the end are no-ops on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "armon_gb300.h"
+#include "host_common.h"
+#include "launch.h"
+
+using namespace armon;
+
+struct armon_solver {
+    armon_params p{};
+    armon_solver_opts o{};
+    int device = 0;
+    int sm_count = 152;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool fp32 = false;
+    size_t elem = 8;
+    void* arr[16] = {};
+    bool owns_arrays = false;
+    StepState* d_state = nullptr;
+    StepState* h_state = nullptr;   // pinned
+    double* d_partials = nullptr;
+    double* d_cons = nullptr;       // conservation partials + 2 results
+    int cons_grid = 0;
+    StepConfig cfg{};
+    SweepArgs<double> a64{};
+    SweepArgs<float> a32{};
+    int grid = 0, block = 128, npass = 2;
+    cudaGraphExec_t graph = nullptr;
+    int graph_cycles = 0;
+    int64_t launches = 0;
+    bool begun = false;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return ARMON_ERR_CUDA;
+}
+
+#define CUDA_TRY(expr)                                            \
+    do {                                                          \
+        cudaError_t e_ = (expr);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);       \
+    } while (0)
+
+// Cells the fused pass reads beyond the real ones along its axis: the reference's flux domain
+// (src/ranges.cpp:14-30) reaches one cell further than min_ghosts except for GAD + second order.
+int stencil_reach(const armon_params* p)
+{
+    return 2 + (p->scheme == ARMON_GAD) + (p->projection == ARMON_EULER_2ND);
+}
+
+bool is_pow2(double x)
+{
+    int e;
+    double m = std::frexp(x, &e);
+    return x > 0 && m == 0.5;
+}
+
+// Segments along the axis: minimise (most blocks on one SM) x (cells a thread walks, halo
+// included) over the segment count, with segments of at least 16 cells.
+void choose_segments(int n, int nlines, int block, int halo, int sms, int forced, int* seg_len, int* nseg, int* nlb)
+{
+    *nlb = std::max(1, (nlines + block - 1) / block);
+    if (forced > 0) {
+        *seg_len = std::min(forced, n);
+        *nseg = (n + *seg_len - 1) / *seg_len;
+        return;
+    }
+    double best = 1e300;
+    int best_seg = n;
+    for (int ns = 1; ns <= std::max(1, n / 16); ns++) {
+        int sl = (n + ns - 1) / ns;
+        if ((int64_t)sl * (ns - 1) >= n) continue;
+        int64_t blocks = (int64_t)(*nlb) * ns;
+        double per_sm = std::ceil(double(blocks) / sms);
+        double cost = per_sm * (sl + 1.2 * halo);
+        if (cost < best - 1e-9) { best = cost; best_seg = sl; }
+    }
+    *seg_len = best_seg;
+    *nseg = (n + best_seg - 1) / best_seg;
+}
+
+template <class T>
+void fill_geom(armon_solver* s, SweepArgs<T>& a)
+{
+    const armon_params& p = s->p;
+    const int halo = stencil_reach(&p);
+    for (int axis = 0; axis < 2; axis++) {
+        AxisGeom<T>& g = a.geom[axis];
+        g.n = axis == 0 ? p.nx : p.ny;
+        g.nlines = axis == 0 ? p.ny : p.nx;
+        g.s = axis == 0 ? 1 : p.row_length;
+        g.lstride = axis == 0 ? p.row_length : 1;
+        choose_segments(g.n, g.nlines, s->block, halo, s->sm_count, s->o.seg_len, &g.seg_len, &g.nseg, &g.nlb);
+        g.blocks = g.nlb * g.nseg;
+        // BC sign factors: X pass low = Left, high = Right; Y pass low = Bottom (y = -1), high = Top.
+        double lo_u, lo_v, hi_u, hi_v;
+        armon_boundary_factors(p.test, axis == 0 ? ARMON_LEFT : ARMON_BOTTOM, &lo_u, &lo_v);
+        armon_boundary_factors(p.test, axis == 0 ? ARMON_RIGHT : ARMON_TOP, &hi_u, &hi_v);
+        // axis velocity: umat in X, vmat in Y
+        g.fa_lo = T(axis == 0 ? lo_u : lo_v);
+        g.fo_lo = T(axis == 0 ? lo_v : lo_u);
+        g.fa_hi = T(axis == 0 ? hi_u : hi_v);
+        g.fo_hi = T(axis == 0 ? hi_v : hi_u);
+        double dx = (axis == 0 ? p.domain_size[0] / double(p.nx) : p.domain_size[1] / double(p.ny));
+        g.dx = T(dx);
+        g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;
+        g.inv_dx = g.dx_pow2 ? T(1.0 / double(g.dx)) : T(0);
+    }
+    a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
+    a.sw = p.stencil_width;
+    a.limiter = p.limiter;
+    a.npass = s->npass;
+    a.write_eos = 1;
+    a.gamma = T(1.4);   // update_EOS hard-codes gamma = 1.4 (src/armon_2D.cpp:94)
+    T* const* arr = reinterpret_cast<T* const*>(s->arr);
+    // set 0: rho umat vmat Emat; set 1: the four work arrays (free in the fused path)
+    a.buf[0][0] = arr[2]; a.buf[0][1] = arr[3]; a.buf[0][2] = arr[4]; a.buf[0][3] = arr[5];
+    a.buf[1][0] = arr[11]; a.buf[1][1] = arr[12]; a.buf[1][2] = arr[13]; a.buf[1][3] = arr[14];
+    a.pmat = arr[6]; a.cmat = arr[7]; a.gmat = arr[8];
+    a.state = s->d_state;
+    a.cfg = s->cfg;
+    a.partials = s->d_partials;
+    s->grid = std::max(a.geom[0].blocks, a.geom[1].blocks);
+}
+
+int check_supported(const armon_params* p)
+{
+    if (!armon_params_check(p)) { set_error("invalid parameters (Params::check)"); return ARMON_ERR_PARAMS; }
+    if (p->test == ARMON_BIZARRIUM) {
+        set_error("the fused solver implements the perfect-gas EOS only (Bizarrium is served by the stage kernels)");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    if (p->projection == ARMON_PROJ_NONE) { set_error("projection None is not supported"); return ARMON_ERR_UNSUPPORTED; }
+    const int halo = stencil_reach(p);
+    if (p->nb_ghosts < halo) {
+        set_error("the fused solver needs nb_ghosts >= " + std::to_string(halo) + " for this scheme");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    if (p->nx < p->stencil_width || p->ny < p->stencil_width) {
+        set_error("the fused solver needs nx, ny >= stencil_width (mirrored bands may not overlap)");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    return ARMON_OK;
+}
+
+int sync_state(armon_solver* s)
+{
+    CUDA_TRY(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return ARMON_OK;
+}
+
+int enqueue_direct(armon_solver* s, int n_cycles)
+{
+    for (int c = 0; c < n_cycles; c++) {
+        for (int k = 0; k < s->npass; k++) {
+            bool last = k == s->npass - 1;
+            cudaError_t e;
+            if (s->fp32) {
+                s->a32.pass = k;
+                e = launch_sweep(s->a32, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
+            } else {
+                s->a64.pass = k;
+                e = launch_sweep(s->a64, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+            s->launches++;
+        }
+    }
+    return ARMON_OK;
+}
+
+int build_graph(armon_solver* s)
+{
+    if (s->graph || s->graph_cycles <= 0) return ARMON_OK;
+    cudaGraph_t g = nullptr;
+    int64_t saved = s->launches;
+    CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_direct(s, s->graph_cycles);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    s->launches = saved;
+    if (rc != ARMON_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { s->graph = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+    return ARMON_OK;
+}
+
+int enqueue(armon_solver* s, int n_cycles)
+{
+    if (s->graph_cycles > 0 && n_cycles >= s->graph_cycles) {
+        int rc = build_graph(s);
+        if (rc != ARMON_OK) return rc;
+        while (n_cycles >= s->graph_cycles) {
+            CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
+            s->launches += (int64_t)s->graph_cycles * s->npass;
+            n_cycles -= s->graph_cycles;
+        }
+    }
+    return enqueue_direct(s, n_cycles);
+}
+
+// Puts the current state back into set 0 (rho, umat, vmat, Emat) so that the reference's
+// arrays hold it, as after the reference's time loop.
+int settle(armon_solver* s)
+{
+    const StepState& st = *s->h_state;
+    int cur = (int)(((int64_t)st.cycle * s->npass + st.buf_base) & 1);
+    if (cur == 0) return ARMON_OK;
+    size_t bytes = (size_t)s->p.nb_cells * s->elem;
+    for (int k = 0; k < 4; k++)
+        CUDA_TRY(cudaMemcpyAsync(s->arr[2 + k], s->arr[11 + k], bytes, cudaMemcpyDeviceToDevice, s->stream));
+    s->h_state->buf_base = (int)(((int64_t)st.cycle * s->npass) & 1);
+    CUDA_TRY(cudaMemcpyAsync(&s->d_state->buf_base, &s->h_state->buf_base, sizeof(int32_t),
+                             cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return ARMON_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void armon_solver_opts_default(armon_solver_opts* o)
+{
+    std::memset(o, 0, sizeof(*o));
+    o->precision = 64;
+    o->cycles_per_graph = 16;
+    o->materialize_eos = 1;
+}
+
+int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, void* stream, armon_solver** out)
+{
+    *out = nullptr;
+    int rc = check_supported(p);
+    if (rc != ARMON_OK) return rc;
+    armon_solver* s = new armon_solver();
+    s->p = *p;
+    if (opts) s->o = *opts; else armon_solver_opts_default(&s->o);
+    if (s->o.precision != 32 && s->o.precision != 64) { delete s; set_error("precision must be 32 or 64"); return ARMON_ERR_PARAMS; }
+    s->fp32 = s->o.precision == 32;
+    s->elem = s->fp32 ? 4 : 8;
+    s->block = s->o.block_lines > 0 ? s->o.block_lines : 128;
+    if (s->block % 32 != 0 || s->block > 128) { delete s; set_error("block_lines must be a multiple of 32, at most 128"); return ARMON_ERR_PARAMS; }
+    s->graph_cycles = s->o.cycles_per_graph;
+    s->npass = passes_per_cycle(p->axis_splitting);
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) { delete s; return cuda_fail(e, "cudaGetDevice"); }
+    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete s; return cuda_fail(e, "cudaStreamCreate"); }
+        s->own_stream = true;
+    }
+    size_t bytes = (size_t)p->nb_cells * s->elem;
+    s->owns_arrays = true;
+    for (int k = 0; k < 16; k++) {
+        e = cudaMalloc(&s->arr[k], bytes);
+        if (e != cudaSuccess) {
+            armon_solver_destroy(s);
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return ARMON_ERR_NOMEM;
+        }
+    }
+    e = cudaMalloc(&s->d_state, sizeof(StepState));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_state, sizeof(StepState));
+    // the partial buffers are sized after the geometry is known
+    s->cfg.cfl = p->cfl;
+    s->cfg.Dt = p->Dt;
+    s->cfg.max_time = p->max_time;
+    s->cfg.dt_dx = p->domain_size[0] / double(p->nx);
+    s->cfg.dt_dy = p->domain_size[1] / double(p->ny);
+    s->cfg.cst_dt = p->cst_dt;
+    s->cfg.dt_on_even_cycles = p->dt_on_even_cycles;
+    s->cfg.max_cycles = p->max_cycles;
+    s->cfg.splitting = p->axis_splitting;
+    if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
+    int pblocks = std::max(s->grid, s->sm_count * 8);
+    s->cons_grid = s->sm_count * 4;
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)pblocks);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_cons, sizeof(double) * (2 * (size_t)s->cons_grid + 2));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
+    if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
+    std::memset(s->h_state, 0, sizeof(StepState));
+    if (s->fp32) { s->a32.state = s->d_state; s->a32.partials = s->d_partials; s->a32.write_eos = s->o.materialize_eos; }
+    else { s->a64.state = s->d_state; s->a64.partials = s->d_partials; s->a64.write_eos = s->o.materialize_eos; }
+    *out = s;
+    return ARMON_OK;
+}
+
+void armon_solver_destroy(armon_solver* s)
+{
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->owns_arrays)
+        for (auto& a : s->arr) if (a) cudaFree(a);
+    if (s->d_state) cudaFree(s->d_state);
+    if (s->h_state) cudaFreeHost(s->h_state);
+    if (s->d_partials) cudaFree(s->d_partials);
+    if (s->d_cons) cudaFree(s->d_cons);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int armon_solver_begin_loop(armon_solver* s)
+{
+    // time_loop's start (src/armon_2D.cpp:327-346): cycle = 0, time = 0, dts = 0, update_axis(X),
+    // update_EOS, and here also the cycle-0 dt_CFL.  The shadow set starts as a copy of the state
+    // so that its untouched ghost cells hold the same values.
+    if (s->begun) {
+        int rc = sync_state(s);
+        if (rc == ARMON_OK) rc = settle(s);
+        if (rc != ARMON_OK) return rc;
+    }
+    size_t bytes = (size_t)s->p.nb_cells * s->elem;
+    for (int k = 0; k < 4; k++)
+        CUDA_TRY(cudaMemcpyAsync(s->arr[11 + k], s->arr[2 + k], bytes, cudaMemcpyDeviceToDevice, s->stream));
+    BeginArgs b{};
+    b.nx = s->p.nx; b.ny = s->p.ny;
+    b.origin = (int64_t)s->p.nb_ghosts * s->p.row_length + s->p.nb_ghosts;
+    b.row_length = s->p.row_length;
+    b.gamma = 1.4;
+    b.rho = s->arr[2]; b.umat = s->arr[3]; b.vmat = s->arr[4]; b.Emat = s->arr[5];
+    b.pmat = s->arr[6]; b.cmat = s->arr[7]; b.gmat = s->arr[8];
+    b.state = s->d_state;
+    b.cfg = s->cfg;
+    b.partials = s->d_partials;
+    b.buf_base = 0;
+    CUDA_TRY(cudaMemsetAsync(&s->d_state->counter, 0, sizeof(uint32_t), s->stream));
+    CUDA_TRY(launch_begin(b, s->fp32, s->sm_count * 4, s->stream));
+    s->launches++;
+    s->begun = true;
+    return sync_state(s);
+}
+
+int armon_solver_init_test(armon_solver* s)
+{
+    const armon_params& p = s->p;
+    InitArgs a{};
+    a.row_length = p.row_length; a.nb_ghosts = p.nb_ghosts; a.nx = p.nx; a.ny = p.ny;
+    a.pos_x = 0; a.pos_y = 0; a.g_nx = p.nx; a.g_ny = p.ny;
+    a.sx = p.domain_size[0]; a.sy = p.domain_size[1]; a.ox = p.domain_origin[0]; a.oy = p.domain_origin[1];
+    double dx = p.domain_size[0] / double(p.nx), dy = p.domain_size[1] / double(p.ny);
+    a.test_option = armon_test_option(&p, dx, dy);
+    a.test = p.test;
+    a.debug_indexes = 0;
+    a.tp = make_test_params(p.test, a.test_option);
+    InitPtrs ptr{s->arr[0], s->arr[1], s->arr[2], s->arr[5], s->arr[3], s->arr[4], s->arr[15],
+                 s->arr[6], s->arr[7], s->arr[8], s->arr[9], s->arr[10]};
+    CUDA_TRY(launch_init(a, p.nb_cells, ptr, s->fp32, s->stream));
+    s->launches++;
+    return armon_solver_begin_loop(s);
+}
+
+int armon_solver_enqueue_cycles(armon_solver* s, int n_cycles)
+{
+    if (!s->begun) { set_error("the time loop has not been started (init_test / begin_loop)"); return ARMON_ERR_STATE; }
+    return enqueue(s, n_cycles);
+}
+
+int armon_solver_run(armon_solver* s, int cycle_limit)
+{
+    if (!s->begun) { set_error("the time loop has not been started (init_test / begin_loop)"); return ARMON_ERR_STATE; }
+    int rc = sync_state(s);
+    if (rc != ARMON_OK) return rc;
+    int issued = 0;
+    for (;;) {
+        const StepState& st = *s->h_state;
+        if (st.status == STATUS_INVALID_DT) {
+            set_error("invalid dt at cycle " + std::to_string(st.cycle));
+            return ARMON_ERR_INVALID_DT;
+        }
+        bool running = st.time < s->cfg.max_time && st.cycle < s->cfg.max_cycles;
+        if (!running || (cycle_limit > 0 && issued >= cycle_limit)) break;
+        // at most the cycles left before max_cycles; when time decides, one graph batch at a time
+        int left = s->cfg.max_cycles - st.cycle;
+        int n = std::min(left, s->graph_cycles > 0 ? s->graph_cycles : 16);
+        if (cycle_limit > 0) n = std::min(n, cycle_limit - issued);
+        rc = enqueue(s, n);
+        if (rc != ARMON_OK) return rc;
+        issued += n;
+        rc = sync_state(s);
+        if (rc != ARMON_OK) return rc;
+    }
+    return settle(s);
+}
+
+int armon_solver_sync_params(armon_solver* s, armon_params* p, int32_t* status)
+{
+    int rc = sync_state(s);
+    if (rc != ARMON_OK) return rc;
+    const StepState& st = *s->h_state;
+    *p = s->p;
+    p->cycle = st.cycle;
+    p->time = st.time;
+    p->current_cycle_dt = st.current_dt;
+    p->next_cycle_dt = st.next_dt;
+    if (status) *status = st.status;
+    return ARMON_OK;
+}
+
+static int current_index(armon_solver* s, int which)
+{
+    // rho, umat, vmat, Emat live in the set the last pass wrote
+    if (which < 2 || which > 5) return which;
+    const StepState& st = *s->h_state;
+    int cur = (int)(((int64_t)st.cycle * s->npass + st.buf_base) & 1);
+    return cur ? which + 9 : which;
+}
+
+int armon_solver_download(armon_solver* s, int which, double* host)
+{
+    if (which < 0 || which > 15) { set_error("array index out of range"); return ARMON_ERR_PARAMS; }
+    int rc = sync_state(s);
+    if (rc != ARMON_OK) return rc;
+    int k = current_index(s, which);
+    size_t n = (size_t)s->p.nb_cells;
+    if (!s->fp32) {
+        CUDA_TRY(cudaMemcpyAsync(host, s->arr[k], n * 8, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return ARMON_OK;
+    }
+    std::vector<float> tmp(n);
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), s->arr[k], n * 4, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (size_t i = 0; i < n; i++) host[i] = tmp[i];
+    return ARMON_OK;
+}
+
+int armon_solver_upload(armon_solver* s, int which, const double* host)
+{
+    if (which < 0 || which > 15) { set_error("array index out of range"); return ARMON_ERR_PARAMS; }
+    int rc = sync_state(s);
+    if (rc != ARMON_OK) return rc;
+    int k = current_index(s, which);
+    size_t n = (size_t)s->p.nb_cells;
+    if (!s->fp32) {
+        CUDA_TRY(cudaMemcpyAsync(s->arr[k], host, n * 8, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        return ARMON_OK;
+    }
+    std::vector<float> tmp(n);
+    for (size_t i = 0; i < n; i++) tmp[i] = (float)host[i];
+    CUDA_TRY(cudaMemcpyAsync(s->arr[k], tmp.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return ARMON_OK;
+}
+
+double* armon_solver_device_array(armon_solver* s, int which)
+{
+    if (s->fp32 || which < 0 || which > 15) return nullptr;
+    if (sync_state(s) != ARMON_OK) return nullptr;
+    return (double*)s->arr[current_index(s, which)];
+}
+
+int armon_solver_conservation(armon_solver* s, double* mass, double* energy)
+{
+    int rc = sync_state(s);
+    if (rc != ARMON_OK) return rc;
+    ConsArgs a{};
+    a.nx = s->p.nx; a.ny = s->p.ny;
+    a.origin = (int64_t)s->p.nb_ghosts * s->p.row_length + s->p.nb_ghosts;
+    a.row_length = s->p.row_length;
+    // conservation_vars uses p.dx of the current axis (src/armon_2D.cpp:293): after a full loop
+    // the driver's current axis is the last pass's axis.
+    int axis = 0;
+    if (s->h_state->cycle > 0) {
+        double f;
+        split_axis(s->p.axis_splitting, s->h_state->cycle - 1, s->npass - 1, &axis, &f);
+    }
+    double dx = axis == 0 ? s->p.domain_size[0] / double(s->p.nx) : s->p.domain_size[1] / double(s->p.ny);
+    a.ds = dx * dx;
+    a.rho = s->arr[current_index(s, 2)];
+    a.Emat = s->arr[current_index(s, 5)];
+    a.partials = s->d_cons;
+    a.out = s->d_cons + 2 * s->cons_grid;
+    CUDA_TRY(launch_conservation(a, s->fp32, s->cons_grid, s->stream));
+    double out[2];
+    CUDA_TRY(cudaMemcpyAsync(out, a.out, sizeof(out), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    *mass = out[0];
+    *energy = out[1];
+    return ARMON_OK;
+}
+
+int64_t armon_solver_kernel_launches(armon_solver* s) { return s->launches; }
+
+int armon_solve_host(const armon_params* p, const armon_solver_opts* opts, const double* const in[4],
+                     double* const out[5], armon_params* final_state)
+{
+    armon_solver* s = nullptr;
+    int rc = armon_solver_create(p, opts, nullptr, &s);
+    if (rc != ARMON_OK) return rc;
+    rc = armon_solver_init_test(s);                 // geometry, mask and the ghosts of init_test
+    static const int which_in[4] = {2, 3, 4, 5};
+    for (int k = 0; k < 4 && rc == ARMON_OK; k++)
+        if (in && in[k]) rc = armon_solver_upload(s, which_in[k], in[k]);
+    if (rc == ARMON_OK && in) rc = armon_solver_begin_loop(s);
+    if (rc == ARMON_OK) rc = armon_solver_run(s, 0);
+    static const int which_out[5] = {2, 3, 4, 5, 6};
+    for (int k = 0; k < 5 && rc == ARMON_OK; k++)
+        if (out && out[k]) rc = armon_solver_download(s, which_out[k], out[k]);
+    if (rc == ARMON_OK && final_state) rc = armon_solver_sync_params(s, final_state, nullptr);
+    armon_solver_destroy(s);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,414 @@
+// sweep.cuh -- the fused axis pass: one kernel does the whole per-axis stage sequence of
+// solver_cycle (src/armon_2D.cpp:304-324) for every real cell:
+//
+//   perfect_gas_EOS     src/kernels/fluid_eos.cpp:9-23
+//   boundary_conditions src/kernels/halo_exchange.cpp:9-36     (ghosts made on the fly)
+//   acoustic / _GAD     src/kernels/acoustic.cpp:10-108
+//   cell_update         src/kernels/euler_projection.cpp:9-22
+//   advection 1st / 2nd src/kernels/euler_projection.cpp:51-120
+//   euler_projection    src/kernels/euler_projection.cpp:25-48
+//   dt_CFL (last pass)  src/kernels/reductions.cpp:8-24
+//
+// Mapping.  A thread owns one line (a row for the X pass, a column for the Y pass) and a segment
+// [a, b) of its real cells, and marches t = a - H .. b - 1 + H along the line (H = the stencil
+// reach: 4 for GAD + second-order remap).  Each step loads one cell and advances a register
+// pipeline by one position: EOS(t), Godunov face t, GAD face t-1, Lagrange cell t-2, advection face
+// t-3, projection cell t-4.  Every intermediate (face flux, Lagrangian cell, product rho*u, the
+// Lagrangian width dx + dt*(u*[i+1] - u*[i])) is computed once and reused from the window, so the
+// FP64 work per cell is the reference's minus its recomputation.  Threads of a warp own adjacent
+// lines, so the Y pass reads coalesced rows.
+//
+// Exactness.  Every value is computed with the reference's expression tree; the file is compiled
+// with --fmad=false, so results are bit-identical to the reference's strict build.  Reuse only
+// replaces a recomputation of the same expression on the same inputs.  Division by dx becomes a
+// multiplication only when dx is a power of two (then both are exact scalings).
+//
+// Ghosts.  Positions -sw..-1 and n..n+sw-1 are the mirror images of real cells with the sign
+// factors of the side (what boundary_conditions writes); EOS of a mirrored state equals the copied
+// EOS of its source since (-u)^2 == u^2.  Positions beyond the stencil width keep the values in
+// memory, as in the reference, where boundary_conditions never writes them.  Ghost memory is never
+// written here.
+//
+// State.  Each pass reads one buffer set and writes the other (in-place updates would race across
+// segment halos); the current set is (cycles_done * passes_per_cycle) % 2.  The pass also writes
+// p, c, g of its input (what update_EOS leaves in memory) for the real cells when asked.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace armon {
+
+template <class T>
+struct AxisGeom {
+    int32_t n;          // real cells along the axis
+    int32_t nlines;     // lines (rows for X, columns for Y)
+    int32_t seg_len;    // real cells per thread
+    int32_t nseg;       // segments per line
+    int32_t nlb;        // blocks of lines (ceil(nlines / blockDim.x))
+    int32_t blocks;     // nlb * nseg
+    int64_t s;          // stride along the axis
+    int64_t lstride;    // stride between lines
+    T fa_lo, fo_lo, fa_hi, fo_hi;   // sign factors of the axis / other velocity, low / high side
+    T dx, inv_dx;       // p.dx of the axis; 1/dx when dx is a power of two
+    int32_t dx_pow2;
+    int32_t pad;
+};
+
+template <class T>
+struct SweepArgs {
+    AxisGeom<T> geom[2];              // X, Y
+    int64_t origin;                   // linear index of real cell (0, 0)
+    int32_t sw;                       // stencil width (depth of the mirrored band)
+    int32_t limiter;                  // 0 None, 1 Minmod, 2 Superbee
+    int32_t pass;                     // pass index within the cycle
+    int32_t npass;                    // passes per cycle
+    int32_t write_eos;                // materialise p, c, g of the real cells
+    int32_t pad;
+    T gamma;
+    T* buf[2][4];                     // two state sets: rho, umat, vmat, Emat
+    T *pmat, *cmat, *gmat;
+    StepState* state;
+    StepConfig cfg;
+    double* partials;                 // 2 doubles per block (dt reduction)
+};
+
+template <class T> struct CellIn { T rho, ua, uo, E, p, c; };
+template <class T> struct God { T us, ps, rcs; };            // rcs = rho_l c_l + rho_r c_r
+template <class T> struct Flux { T us, ps, psus, dtus; };    // psus = p* u*, dtus = dt u*
+template <class T> struct Lag { T rho, ua, uo, E, rua, ruo, rE, W, c; };
+template <class T> struct Adv { T r, ra, ro, rE; };
+
+template <class T>
+__device__ __forceinline__ T limiter_fn(int L, T r)
+{
+    // src/kernels/limiters.h:15-34
+    if (L == 1) return kmax(T(0), kmin(T(1), r));
+    if (L == 2) return kmax(kmax(T(0), kmin(T(1), 2 * r)), kmin(T(2), r));
+    return T(1);
+}
+
+template <class T>
+__device__ __forceinline__ T slope_minmod(T u_im, T u_i, T u_ip, T r_m, T r_p)
+{
+    // src/kernels/euler_projection.cpp:73-79
+    T D_u_p = r_p * (u_ip - u_i);
+    T D_u_m = r_m * (u_i - u_im);
+    T s = copysign(T(1), D_u_p);
+    return s * kmax(T(0), kmin(s * D_u_p, s * D_u_m));
+}
+
+template <class T>
+__device__ __forceinline__ T apply_factor(T v, T f)
+{
+    // u * factor for the sign factors +-1 without an FP multiply (exact for non-NaN v)
+    return f == T(1) ? v : (f == T(-1) ? -v : v * f);
+}
+
+template <class T>
+__device__ __forceinline__ T div_dx(T x, const AxisGeom<T>& g)
+{
+    return g.dx_pow2 ? x * g.inv_dx : x / g.dx;
+}
+
+template <class T>
+__device__ __forceinline__ void eos(CellIn<T>& c, T gamma)
+{
+    // src/kernels/fluid_eos.cpp:18-21
+    T e = c.E - T(0.5) * (c.ua * c.ua + c.uo * c.uo);
+    c.p = (gamma - 1) * c.rho * e;
+    c.c = sqrt(gamma * c.p / c.rho);
+}
+
+template <class T>
+__device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R)
+{
+    // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i)
+    God<T> g;
+    T rc_l = L.rho * L.c;
+    T rc_r = R.rho * R.c;
+    g.rcs = rc_l + rc_r;
+    g.us = (rc_l * L.ua + rc_r * R.ua + (L.p - R.p)) / g.rcs;
+    g.ps = (rc_r * L.p + rc_l * R.p + rc_l * rc_r * (L.ua - R.ua)) / g.rcs;
+    return g;
+}
+
+template <class T>
+__device__ __forceinline__ Flux<T> gad(const God<T>& Gm, const God<T>& Gc, const God<T>& Gp,
+                                       const CellIn<T>& Cl, const CellIn<T>& Cr, int L, T dt, T dx)
+{
+    // src/kernels/acoustic.cpp:40-88 (face between Cl = i-s and Cr = i)
+    T r_um = (Gp.us - Cr.ua) / (Gc.us - Cl.ua + T(1e-6));
+    T r_pm = (Gp.ps - Cr.p) / (Gc.ps - Cl.p + T(1e-6));
+    T r_up = (Cl.ua - Gm.us) / (Cr.ua - Gc.us + T(1e-6));
+    T r_pp = (Cl.p - Gm.ps) / (Cr.p - Gc.ps + T(1e-6));
+    r_um = limiter_fn(L, r_um);
+    r_pm = limiter_fn(L, r_pm);
+    r_up = limiter_fn(L, r_up);
+    r_pp = limiter_fn(L, r_pp);
+    T dm_l = Cl.rho * dx;
+    T dm_r = Cr.rho * dx;
+    T Dm = (dm_l + dm_r) * T(0.5);                       // (dm_l + dm_r) / 2
+    T theta = T(0.5) * (1 - (Gc.rcs * T(0.5)) * (dt / Dm));
+    Flux<T> f;
+    f.us = Gc.us + theta * (r_up * (Cr.ua - Gc.us) - r_um * (Gc.us - Cl.ua));
+    f.ps = Gc.ps + theta * (r_pp * (Cr.p - Gc.ps) - r_pm * (Gc.ps - Cl.p));
+    return f;
+}
+
+template <class T>
+__device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0, const Flux<T>& F1, T dt, T dx)
+{
+    // src/kernels/euler_projection.cpp:9-22 for cell i (F0 = face i, F1 = face i+s)
+    Lag<T> l;
+    T dm = C.rho * dx;
+    l.W = dx + dt * (F1.us - F0.us);
+    l.rho = dm / l.W;
+    T dtdm = dt / dm;
+    l.ua = C.ua + dtdm * (F0.ps - F1.ps);
+    l.E = C.E + dtdm * (F0.psus - F1.psus);
+    l.uo = C.uo;
+    l.rua = l.rho * l.ua;
+    l.ruo = l.rho * l.uo;
+    l.rE = l.rho * l.E;
+    l.c = C.c;
+    return l;
+}
+
+template <class T>
+__device__ __forceinline__ Lag<T> sel(bool p, const Lag<T>& a, const Lag<T>& b)
+{
+    Lag<T> r;
+    r.rho = p ? a.rho : b.rho; r.ua = p ? a.ua : b.ua; r.uo = p ? a.uo : b.uo; r.E = p ? a.E : b.E;
+    r.rua = p ? a.rua : b.rua; r.ruo = p ? a.ruo : b.ruo; r.rE = p ? a.rE : b.rE;
+    r.W = p ? a.W : b.W; r.c = p ? a.c : b.c;
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, const Flux<T>& Fp,
+                                          const Lag<T>& L0, const Lag<T>& L1, const Lag<T>& L2, const Lag<T>& L3,
+                                          T dx)
+{
+    // src/kernels/euler_projection.cpp:82-120 for face k; L0..L3 = cells k-2..k+1
+    T disp = Fk.dtus;
+    bool up = disp > 0;
+    T Dx = up ? -(dx - Fm.dtus) : dx + Fp.dtus;
+    Lag<T> Cm = sel(up, L0, L1), Ci = sel(up, L1, L2), Cp = sel(up, L2, L3);
+    T Dx_lm = Cm.W, Dx_l = Ci.W, Dx_lp = Cp.W;
+    T r_m = (2 * Dx_l) / (Dx_l + Dx_lm);
+    T r_p = (2 * Dx_l) / (Dx_l + Dx_lp);
+    T slope_r = slope_minmod(Cm.rho, Ci.rho, Cp.rho, r_m, r_p);
+    T slope_ra = slope_minmod(Cm.rua, Ci.rua, Cp.rua, r_m, r_p);
+    T slope_ro = slope_minmod(Cm.ruo, Ci.ruo, Cp.ruo, r_m, r_p);
+    T slope_rE = slope_minmod(Cm.rE, Ci.rE, Cp.rE, r_m, r_p);
+    T length_factor = Dx / (2 * Dx_l);
+    Adv<T> a;
+    a.r = disp * (Ci.rho - slope_r * length_factor);
+    a.ra = disp * (Ci.rua - slope_ra * length_factor);
+    a.ro = disp * (Ci.ruo - slope_ro * length_factor);
+    a.rE = disp * (Ci.rE - slope_rE * length_factor);
+    return a;
+}
+
+template <class T>
+__device__ __forceinline__ Adv<T> advect1(const Flux<T>& Fk, const Lag<T>& Lm, const Lag<T>& Lk)
+{
+    // src/kernels/euler_projection.cpp:51-70 for face k (Lm = cell k-s, Lk = cell k)
+    T disp = Fk.dtus;
+    bool up = disp > 0;
+    Adv<T> a;
+    a.r = disp * (up ? Lm.rho : Lk.rho);
+    a.ra = disp * (up ? Lm.rua : Lk.rua);
+    a.ro = disp * (up ? Lm.ruo : Lk.ruo);
+    a.rE = disp * (up ? Lm.rE : Lk.rE);
+    return a;
+}
+
+// Scheme 0 Godunov / 1 GAD; Proj 1 first order / 2 second order; LAST: the pass that ends a cycle.
+template <class T, int SCHEME, int PROJ, bool LAST>
+__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
+{
+    constexpr bool kGAD = SCHEME == 1;
+    constexpr bool kE2 = PROJ == 2;
+    constexpr int LAG_F = kGAD ? 1 : 0;             // flux face = t - LAG_F
+    constexpr int LAG_L = LAG_F + 1;                // Lagrange cell
+    constexpr int LAG_A = kE2 ? LAG_F + 2 : LAG_L;  // advection face
+    constexpr int H = LAG_A + 1;                    // projection lag == stencil reach
+
+    __shared__ double red[2][4];
+    __shared__ int is_last_block;
+
+    const StepState st = *A.state;
+    const CycleDt cd = cycle_time_step(st, A.cfg);
+    if (!cd.run) return;
+    if (cd.invalid) {
+        if (LAST && blockIdx.x == 0 && threadIdx.x == 0) A.state->status = STATUS_INVALID_DT;
+        return;
+    }
+
+    int axis;
+    double factor;
+    split_axis(A.cfg.splitting, st.cycle, A.pass, &axis, &factor);
+    const AxisGeom<T>& g = A.geom[axis];
+    const T dt = T(cd.current * factor);
+    const T dx = g.dx;
+    const int src = (int)(((int64_t)st.cycle * A.npass + A.pass + st.buf_base) & 1);
+    T* const* in = A.buf[src];
+    T* const* out = A.buf[src ^ 1];
+    // X pass: the axis velocity is umat (1), Y pass: vmat (2)
+    const T* __restrict__ rho_in = in[0];
+    const T* __restrict__ ua_in = in[axis == 0 ? 1 : 2];
+    const T* __restrict__ uo_in = in[axis == 0 ? 2 : 1];
+    const T* __restrict__ E_in = in[3];
+
+    DtAcc acc;
+    acc.init();
+
+    const int lb = blockIdx.x % max(g.nlb, 1);
+    const int seg = blockIdx.x / max(g.nlb, 1);
+    const int line = lb * blockDim.x + threadIdx.x;
+    const bool active = blockIdx.x < g.blocks && line < g.nlines;
+
+    if (active) {
+        const int n = g.n, sw = A.sw;
+        const int a0 = seg * g.seg_len;
+        const int b0 = min(n, a0 + g.seg_len);
+        const int64_t base = A.origin + (int64_t)line * g.lstride;
+        const int64_t s = g.s;
+        const int t0 = a0 - H, t1 = b0 - 1 + H;
+        const int firstF = kGAD ? t0 + 2 : t0 + 1;
+
+        CellIn<T> C0{}, C1{}, C2{};
+        God<T> G0{}, G1{}, G2{};
+        Flux<T> F0{}, F1{}, F2{}, F3{}, F4{};
+        Lag<T> L0{}, L1{}, L2{}, L3{};
+        Adv<T> A0{}, A1{};
+
+        for (int t = t0; t <= t1; ++t) {
+            // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
+            C0 = C1; C1 = C2;
+            {
+                CellIn<T> c;
+                bool stale = false;
+                int m = t;
+                T fa = T(1), fo = T(1);
+                if (t < 0) {
+                    if (t >= -sw) { m = -1 - t; fa = g.fa_lo; fo = g.fo_lo; } else stale = true;
+                } else if (t >= n) {
+                    if (t < n + sw) { m = 2 * n - 1 - t; fa = g.fa_hi; fo = g.fo_hi; } else stale = true;
+                }
+                const int64_t idx = base + (int64_t)m * s;
+                c.rho = rho_in[idx];
+                c.ua = apply_factor(ua_in[idx], fa);
+                c.uo = apply_factor(uo_in[idx], fo);
+                c.E = E_in[idx];
+                if (stale) {
+                    c.p = A.pmat[idx];
+                    c.c = A.cmat[idx];
+                } else {
+                    eos(c, A.gamma);
+                    if (m == t && t >= a0 && t < b0 && A.write_eos) {   // owned real cell: what update_EOS stores
+                        A.pmat[idx] = c.p;
+                        A.cmat[idx] = c.c;
+                        A.gmat[idx] = (1 + A.gamma) / 2;
+                    }
+                }
+                C2 = c;
+            }
+            // ---- Godunov face t ----
+            if (t >= t0 + 1) { G0 = G1; G1 = G2; G2 = godunov(C1, C2); }
+            // ---- numerical flux at face f = t - LAG_F ----
+            if (kGAD ? (t >= t0 + 3) : (t >= t0 + 1)) {
+                F0 = F1; F1 = F2; F2 = F3; F3 = F4;
+                Flux<T> f;
+                if (kGAD) {
+                    f = gad(G0, G1, G2, C0, C1, A.limiter, dt, dx);
+                } else {
+                    f.us = G2.us; f.ps = G2.ps;
+                }
+                f.psus = f.ps * f.us;
+                f.dtus = dt * f.us;
+                F4 = f;
+            }
+            // ---- Lagrange update of cell j = t - LAG_L ----
+            const int j = t - LAG_L;
+            if (j >= firstF) {
+                L0 = L1; L1 = L2; L2 = L3;
+                L3 = lagrange(kGAD ? C0 : C1, F3, F4, dt, dx);
+            }
+            // ---- advection flux at face k = t - LAG_A ----
+            const int k = t - LAG_A;
+            if (k >= a0) {
+                A0 = A1;
+                A1 = kE2 ? advect2(F1, F2, F3, L0, L1, L2, L3, dx) : advect1(F3, L2, L3);
+            }
+            // ---- projection of cell mm = k - 1 ----
+            const int mm = k - 1;
+            if (mm >= a0) {
+                const Lag<T>& Lc = kE2 ? L1 : L2;
+                // src/kernels/euler_projection.cpp:36-46
+                T dXr = Lc.W * Lc.rho;
+                T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
+                T tmp_ra = div_dx(dXr * Lc.ua - (A1.ra - A0.ra), g);
+                T tmp_ro = div_dx(dXr * Lc.uo - (A1.ro - A0.ro), g);
+                T tmp_rE = div_dx(dXr * Lc.E - (A1.rE - A0.rE), g);
+                T ua = tmp_ra / tmp_rho, uo = tmp_ro / tmp_rho, E = tmp_rE / tmp_rho;
+                const int64_t idx = base + (int64_t)mm * s;
+                out[0][idx] = tmp_rho;
+                out[axis == 0 ? 1 : 2][idx] = ua;
+                out[axis == 0 ? 2 : 1][idx] = uo;
+                out[3][idx] = E;
+                if (LAST) {
+                    // dt_CFL of the state after this pass, with c from this pass's EOS
+                    if (axis == 0) acc.add(double(ua), double(uo), double(Lc.c));
+                    else acc.add(double(uo), double(ua), double(Lc.c));
+                }
+            }
+        }
+    }
+
+    if (!LAST) return;
+
+    // ---- block reduction of the dt maxima, then the last block commits the cycle ----
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.merge(__shfl_xor_sync(0xffffffffu, acc.ax, o), __shfl_xor_sync(0xffffffffu, acc.ay, o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[0][warp] = acc.ax; red[1][warp] = acc.ay; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ax = red[0][0], ay = red[1][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { ax = kmax(ax, red[0][w]); ay = kmax(ay, red[1][w]); }
+        A.partials[2 * blockIdx.x] = ax;
+        A.partials[2 * blockIdx.x + 1] = ay;
+        __threadfence();
+        unsigned prev = atomicAdd(&A.state->counter, 1u);
+        is_last_block = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last_block) return;
+    __threadfence();
+    DtAcc tot;
+    tot.init();
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        tot.merge(__ldcg(&A.partials[2 * b]), __ldcg(&A.partials[2 * b + 1]));
+    for (int o = 16; o > 0; o >>= 1)
+        tot.merge(__shfl_xor_sync(0xffffffffu, tot.ax, o), __shfl_xor_sync(0xffffffffu, tot.ay, o));
+    __syncthreads();
+    if (lane == 0) { red[0][warp] = tot.ax; red[1][warp] = tot.ay; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ax = red[0][0], ay = red[1][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { ax = kmax(ax, red[0][w]); ay = kmax(ay, red[1][w]); }
+        StepState ns = st;
+        ns.raw_dt = dt_from_maxima(ax, ay, A.cfg.dt_dx, A.cfg.dt_dy);
+        ns.current_dt = cd.current;
+        ns.next_dt = cd.next;
+        ns.time = st.time + cd.current;
+        ns.cycle = st.cycle + 1;
+        ns.counter = 0;
+        *A.state = ns;
+    }
+}
+
+}  // namespace armon

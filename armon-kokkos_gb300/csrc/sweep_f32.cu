@@ -1,0 +1,36 @@
+// sweep_f32.cu -- instantiation of the solver kernels for float storage and arithmetic.
+// Built with FMA contraction: the FP32 variant is compared with the FP64 oracle by tolerance
+// (dt and the conservation sums stay FP64).
+#include "solver_kernels.cuh"
+
+namespace armon {
+
+cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
+                         cudaStream_t st)
+{
+    return launch_sweep_t<float>(a, scheme, proj, last, grid, block, st);
+}
+
+cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st)
+{
+    int64_t blocks = (ncells + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (blocks < 1) blocks = 1;
+    init_kernel<float><<<(int)blocks, 256, 0, st>>>(a, ncells, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin_f32(const BeginArgs& a, int grid, cudaStream_t st)
+{
+    begin_kernel<float><<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_conservation_f32(const ConsArgs& a, int grid, cudaStream_t st)
+{
+    conservation_partial_kernel<float><<<grid, 256, 0, st>>>(a);
+    conservation_final_kernel<<<1, 32, 0, st>>>(a.partials, grid, a.out);
+    return cudaGetLastError();
+}
+
+}  // namespace armon

@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Benchmark of the Armon time step on GB300: cell-updates/s of the fused FP64 solver.
+
+Workload (the single-domain drop-in case): circular Sod on [0,1]^2, 4096 x 4096 real cells, 5 ghost
+layers, FP64, gamma 1.4, rho/p = 1/1 inside radius 0.2 and 0.125/0.1 outside, GAD acoustic fluxes
+with the minmod limiter, second-order Euler remap, Sequential X/Y splitting, CFL 0.6.  A step is one
+solver cycle (dt reduction + X pass + Y pass) over the whole grid; the state (4 x 135 MB per buffer
+set) is larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path (the oracle's OpenMP build with the reference's
+Release flags) on the host cores.  N > 1 runs N independent replicas (one per GPU), weak scaling.
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "armon-kokkos_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "cell-updates/s"
+WORKLOAD = dict(test="Sod_circ", scheme="GAD", projection="euler_2nd", limiter="Minmod", splitting="Sequential",
+                nghost=5, nx=4096, ny=4096, cfl=0.6, max_time=1e9, test_option=0.04)
+BYTES_PER_CELL_UPDATE = 64          # read + write rho, u, v, E once per cycle (FP64)
+
+
+def config(nx: int, ny: int, n: int) -> dict:
+    return {"workload": f"Sod_circ {nx}x{ny} FP64, GAD-minmod + euler_2nd, CFL 0.6, radius 0.2, Sequential splitting",
+            "nx": nx, "ny": ny, "nghost": 5, "gamma": 1.4, "scheme": "GAD", "limiter": "Minmod",
+            "projection": "euler_2nd", "splitting": "Sequential", "cfl": 0.6, "radius": 0.2,
+            "step": "one solver cycle (dt_CFL + X pass + Y pass)",
+            "l2": "inputs larger than L2 (state 4 x %d MB per buffer set)" % ((nx + 10) * (ny + 10) * 8 // 2**20),
+            "parallelism": f"replicas x{n}" if n > 1 else "single domain"}
+
+
+def measured_peaks() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic() -> float | None:
+    """DRAM bytes per sweep launch from the committed ncu summary, scaled to this workload."""
+    path = os.path.join(ROOT, "profiles", "sweep_f64_sod_circ.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_cell_per_pass:\s*([0-9.eE+-]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) >= 9:
+                try:
+                    rows.append(parts)
+                except Exception:
+                    pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        # the busiest GPU (highest power) is ours
+        by_gpu: dict[str, list] = {}
+        for r in rows:
+            by_gpu.setdefault(r[0], []).append(r)
+        gpu = max(by_gpu, key=lambda g: statistics.median(float(r[3]) for r in by_gpu[g] if r[3] not in ("", "[N/A]")))
+        rs = by_gpu[gpu]
+        sm = [float(r[1]) for r in rs]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rs for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rs[0][2]), "reasons": reasons,
+                "samples": len(rs), "power_w_median": statistics.median(float(r[3]) for r in rs)}
+
+
+def dist_info() -> tuple[int, int, int]:
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def cpu_port_throughput(nx: int, ny: int, budget_s: float, max_cycles: int) -> dict:
+    """The oracle's OpenMP build with the reference's Release flags, on the host cores."""
+    import oracle_lib as O
+
+    L = O.lib(fast=True)
+    case = O.Case(**{k: v for k, v in WORKLOAD.items()})
+    case.nx, case.ny = nx, ny
+    p = O.make_params(case, L)
+    st = O.OracleState(p)
+    L.o_init_test_p(C.byref(p), C.byref(st.data), 0)
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    L.o_update_EOS(C.byref(p), C.byref(st.data))
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_cycles:
+        if L.o_solver_cycle(C.byref(p), C.byref(st.data)) != 0:
+            break
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+        n += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    secs = time.perf_counter() - t0
+    return {"value": nx * ny * n / secs, "unit": METRIC, "cores": L.o_num_threads(), "kind": "port",
+            "sample": f"{n} cycles of the {nx}x{ny} workload after init (oracle/armon_oracle.c, -O3 -ffast-math, OpenMP)",
+            "seconds": secs, "cycles": n}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    nx = ny = args.size
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
+    # W untimed cycles are included in the same run as warm-up of caches and page faults
+    import oracle_lib as O
+
+    L = O.lib(fast=True)
+    case = O.Case(**WORKLOAD)
+    case.nx, case.ny = nx, ny
+    p = O.make_params(case, L)
+    st = O.OracleState(p)
+    L.o_init_test_p(C.byref(p), C.byref(st.data), 0)
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    L.o_update_EOS(C.byref(p), C.byref(st.data))
+
+    def cycle():
+        assert L.o_solver_cycle(C.byref(p), C.byref(st.data)) == 0
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+
+    for _ in range(args.warmup):
+        cycle()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cycle()
+    secs = time.perf_counter() - t0
+    value = nx * ny * args.steps / secs
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": config(nx, ny, 1),
+           "cpu_baseline": {"value": value, "unit": METRIC, "cores": L.o_num_threads(), "kind": "port",
+                            "sample": f"{args.steps} timed cycles of the {nx}x{ny} workload on the host cores "
+                                      "(oracle/armon_oracle.c: the reference's unfused stage sequence, OpenMP, "
+                                      "-O3 -funroll-loops -ffast-math)"},
+           "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args) -> None:
+    import numpy as np
+    import torch
+
+    import armon_gb300 as A
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    nx = ny = args.size
+    K, W = args.steps, args.warmup
+    case = A.Case(**WORKLOAD)
+    case.nx, case.ny = nx, ny
+    case.max_cycles = W + K
+    stream = torch.cuda.current_stream()
+    s = A.Solver(case, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    s.init_test()
+    s.enqueue_cycles(W)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    launches0 = s.kernel_launches
+    sampler = ClockSampler() if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.25)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.enqueue_cycles(K)
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1)
+    launches = s.kernel_launches - launches0
+    p, status = s.state()
+    if status != 0 or p.cycle != W + K:
+        raise RuntimeError(f"solver state after the timed region: status {status}, cycle {p.cycle}")
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    cells = nx * ny
+    value = cells * K * world / (ms_max / 1e3)
+
+    # end to end through the C ABI with host buffers: H2D of the initial fields from pinned memory,
+    # the time loop, D2H of rho, u, v, E, p (every step of it inside the timed region)
+    ins = {k: torch.from_numpy(s.download(k)).pin_memory() for k in ("rho", "umat", "vmat", "Emat")}
+    s.close()
+    case_e2e = A.Case(**WORKLOAD)
+    case_e2e.nx, case_e2e.ny = nx, ny
+    case_e2e.max_cycles = K
+    se = A.Solver(case_e2e, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    se.init_test()
+    outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
+            for k in ("rho", "umat", "vmat", "Emat", "pmat")}
+    L = A.lib()
+    barrier()
+    t0 = time.perf_counter()
+    for k, name in enumerate(("rho", "umat", "vmat", "Emat")):
+        A.check(L.armon_solver_upload(se._h, A.ARRAYS.index(name), ins[name].data_ptr()))
+    se.begin_loop()
+    se.run()
+    for name in ("rho", "umat", "vmat", "Emat", "pmat"):
+        A.check(L.armon_solver_download(se._h, A.ARRAYS.index(name), outs[name].data_ptr()))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    pe, st_e = se.state()
+    assert st_e == 0 and pe.cycle == K
+    se.close()
+    nb = se.params.nb_cells if hasattr(se, "params") else (nx + 10) * (ny + 10)
+    e2e_t = torch.tensor([e2e_s], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = cells * K * world / float(e2e_t.item())
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        t_launch = ms_max / 1e3 / (K * 2)
+        achieved = BYTES_PER_CELL_UPDATE / 2 * cells / t_launch / 1e9
+        tr = profiled_traffic()
+        out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic", "config": config(nx, ny, world),
+               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "peak_source": peak_kind,
+                            "traffic": (tr * cells if tr else None),
+                            "kernel": "armon::sweep_kernel<double,1,2,*> (one launch = one axis pass)",
+                            "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE / 2 * cells,
+                            "note": "FP64 arithmetic bound: see fp64_pipe in profiles/"},
+               "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
+                       "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,
+                       "path": "armon_solver_upload x4 (pinned) + begin_loop + run + armon_solver_download x5"},
+               "gpu_launches": launches, "clocks": clocks}
+        if world == 1 and not args.no_cpu:
+            out["cpu_baseline"] = cpu_port_throughput(nx, ny, args.cpu_seconds, 200)
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+/*
+ * armon_gb300.h -- native C ABI of the GB300 Armon time step (libarmon_gb300.so).
+ *
+ * Plain C: POD structs, raw pointers, sizes, int status codes.  No CUDA or C++ types cross
+ * this boundary (streams are passed as void*).  The parameter block mirrors the reference's
+ * Params (src/parameters.h:34-108) field for field, so a caller configures a solve with the
+ * reference's own vocabulary; the solver object plays the part of the reference's DataHolder
+ * (src/data.h:15-43) plus its time loop (src/armon_2D.cpp:327-386), with the state resident in
+ * HBM and the per-cycle dt kept on the device.
+ *
+ * Error behaviour: every call returns ARMON_OK (0) or an ARMON_ERR_* code; armon_last_error()
+ * gives a message.  The reference instead prints and exits on an invalid time step
+ * (src/armon_2D.cpp:238-242); here the solver stops and reports ARMON_ERR_INVALID_DT.
+ */
+#ifndef ARMON_GB300_H
+#define ARMON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* src/kernels/test_cases.h:8-14 */
+enum { ARMON_SOD = 0, ARMON_SOD_Y = 1, ARMON_SOD_CIRC = 2, ARMON_BIZARRIUM = 3, ARMON_SEDOV = 4 };
+/* src/parameters.h:17-31, src/kernels/limiters.h:8-12, src/kernels/common.h:30-40 */
+enum { ARMON_GODUNOV = 0, ARMON_GAD = 1 };
+enum { ARMON_PROJ_NONE = 0, ARMON_EULER = 1, ARMON_EULER_2ND = 2 };
+enum { ARMON_LIM_NONE = 0, ARMON_MINMOD = 1, ARMON_SUPERBEE = 2 };
+enum { ARMON_SEQUENTIAL = 0, ARMON_SEQUENTIAL_SYM = 1, ARMON_STRANG = 2, ARMON_X_ONLY = 3, ARMON_Y_ONLY = 4 };
+enum { ARMON_AXIS_X = 0, ARMON_AXIS_Y = 1 };
+enum { ARMON_LEFT = 0, ARMON_RIGHT = 1, ARMON_TOP = 2, ARMON_BOTTOM = 3 };
+
+/* Status codes */
+enum {
+    ARMON_OK = 0,
+    ARMON_ERR_INVALID_DT = 1,   /* a non-finite or non-positive time step (the reference exits) */
+    ARMON_ERR_PARAMS = 2,       /* Params::check failed, or an argument is out of range */
+    ARMON_ERR_CUDA = 3,         /* a CUDA call failed; see armon_last_error() */
+    ARMON_ERR_UNSUPPORTED = 4,  /* a combination this build does not implement */
+    ARMON_ERR_NOMEM = 5,        /* device allocation failed or would exceed the budget */
+    ARMON_ERR_STATE = 6         /* the device step state is inconsistent (e.g. a skipped cycle) */
+};
+
+/* Field list of src/parameters.h:34-108.  Integer fields first, then doubles, so that the
+ * layout has no padding.  `test_option` extends the reference: for Sod_circ it is the squared
+ * radius of the high-pressure disc (0 = the reference's 0.09), for Sedov the blast radius
+ * (0 = derived from dx, dy as the reference does).  The output file name of the reference
+ * (a const char*) is not part of this block. */
+typedef struct armon_params {
+    int32_t test, scheme, riemann, projection, limiter, current_axis, axis_splitting;
+    int32_t nb_ghosts, nx, ny, stencil_width;
+    int32_t cst_dt, dt_on_even_cycles;
+    int32_t row_length, col_length, nb_cells, ideb, ifin, index_start, idx_row, idx_col, s;
+    int32_t cycle, max_cycles;
+    int32_t write_output, write_ghosts, write_throughput, output_precision, verbose, compare;
+    double dx, cfl, Dt;
+    double domain_size[2], domain_origin[2];
+    double cycle_dt, current_cycle_dt, next_cycle_dt, time;
+    double max_time, comparison_tolerance, test_option;
+} armon_params;
+
+/* ---- parameters (src/parameters.cpp) ---- */
+void armon_params_defaults(armon_params* p);          /* member initialisers, src/parameters.h:36-97 */
+void armon_params_init(armon_params* p);              /* Params::init, src/parameters.cpp:21-34 */
+int armon_params_check(const armon_params* p);        /* Params::check: 1 = valid, src/parameters.cpp:70-109 */
+int armon_min_ghosts(const armon_params* p);          /* src/parameters.cpp:11-18 */
+int armon_params_sizeof(void);
+const char* armon_last_error(void);
+int armon_device_count(void);
+
+/* ---- the solver: device-resident state and the fused time loop ---- */
+typedef struct armon_solver armon_solver;
+
+/* Solver options beyond the reference's Params. */
+typedef struct armon_solver_opts {
+    int32_t precision;        /* 64: FP64 state and arithmetic (bit-exact with the reference);
+                                 32: FP32 state and arithmetic, FP64 dt and conservation sums */
+    int32_t cycles_per_graph; /* cycles captured per CUDA graph launch (0 = default, 16) */
+    int32_t seg_len;          /* cells per thread along the sweep axis (0 = automatic) */
+    int32_t block_lines;      /* lines (threads) per block (0 = automatic, 128) */
+    int32_t materialize_eos;  /* write p, c, g of the real cells on every pass (1, default) or only
+                                 on the last pass of a cycle (0) */
+    int32_t reserved[3];
+} armon_solver_opts;
+
+void armon_solver_opts_default(armon_solver_opts* o);
+
+/* Allocates the state of one domain in HBM.  `stream` is a cudaStream_t (NULL = a stream the
+ * solver creates).  The solver keeps a copy of `p`. */
+int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, void* stream,
+                        armon_solver** out);
+void armon_solver_destroy(armon_solver* s);
+
+/* init_test on the device (src/armon_2D.cpp:112-127) followed by the EOS and the first dt
+ * reduction of time_loop (src/armon_2D.cpp:327-346). */
+int armon_solver_init_test(armon_solver* s);
+
+/* Runs cycles until the reference's loop condition (time < max_time && cycle < max_cycles)
+ * fails, or until `cycle_limit` more cycles have been issued (cycle_limit <= 0: no limit).
+ * Asynchronous inputs, synchronous outcome: returns once the device state has been read back. */
+int armon_solver_run(armon_solver* s, int cycle_limit);
+
+/* Enqueues exactly `n_cycles` cycles (no-ops after the loop condition fails) on the solver's
+ * stream without reading anything back; for timing and graph capture by the caller. */
+int armon_solver_enqueue_cycles(armon_solver* s, int n_cycles);
+
+/* Copies the device step state (cycle, time, dts, status) to `p` (blocking). */
+int armon_solver_sync_params(armon_solver* s, armon_params* p, int32_t* status);
+
+/* Host <-> device copies of whole arrays (nb_cells values each, in the reference's layout).
+ * `which` names an array: 0 x, 1 y, 2 rho, 3 umat, 4 vmat, 5 Emat, 6 pmat, 7 cmat, 8 gmat,
+ * 9 ustar, 10 pstar, 11..14 work arrays, 15 domain_mask.  FP32 solvers convert. */
+int armon_solver_download(armon_solver* s, int which, double* host);
+int armon_solver_upload(armon_solver* s, int which, const double* host);
+/* Device pointer of an FP64 array (NULL for an FP32 solver) */
+double* armon_solver_device_array(armon_solver* s, int which);
+
+/* Mass and energy sums over the real cells (src/armon_2D.cpp:287-298), FP64, blocking. */
+int armon_solver_conservation(armon_solver* s, double* mass, double* energy);
+
+/* Number of kernels the solver launched so far (diagnostics). */
+int64_t armon_solver_kernel_launches(armon_solver* s);
+
+/* One full solve with host buffers, the reference-facing end-to-end call: uploads rho, umat,
+ * vmat, Emat (and the rest of the initial state made by init_test on the device), runs the time
+ * loop and downloads rho, umat, vmat, Emat, pmat.  Arrays have nb_cells values in the
+ * reference's layout; `in[k]`/`out[k]` may be NULL to skip one. */
+int armon_solve_host(const armon_params* p, const armon_solver_opts* opts,
+                     const double* const in[4], double* const out[5], armon_params* final_state);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

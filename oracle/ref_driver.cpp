@@ -97,6 +97,11 @@ int main(int argc, char** argv)
 
     Data d(p.nb_cells, "Armon_");
     init_test(p, d);
+    {
+        /* the test option the reference's init_test used (src/armon_2D.cpp:116-118) */
+        flt_t dx = p.domain_size[0] / flt_t(p.nx), dy = p.domain_size[1] / flt_t(p.ny);
+        std::fprintf(stdout, "test_option=%a\n", (double)p.test_case->test_option(dx, dy));
+    }
     dump(p, d, "init_test", 0);
 
     int status = 0;

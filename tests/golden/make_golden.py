@@ -114,6 +114,11 @@ def main() -> None:
         init, final = recs[0], recs[-1]
         p = O.make_params(case)
         kv = dict(tok.split("=") for tok in stdout.split())
+        # The Sedov radius comes from libm's hypot on the host that made the fixtures; record it so
+        # that the fixtures do not depend on another host's libm.
+        topt = float.fromhex(kv["test_option"])
+        if case.test == "Sedov" and case.test_option == 0:
+            case.test_option = topt
         gold["cases"][name] = {
             "case": case.__dict__,
             "cycles": final["cycle"],
@@ -122,6 +127,7 @@ def main() -> None:
             "time": final["time"].hex(),
             "mass": float(kv["mass"]).hex(),
             "energy": float(kv["energy"]).hex(),
+            "reference_test_option": topt.hex(),
             "init_hashes": field_hashes(p, init),
             "hashes": field_hashes(p, final),
         }

@@ -1,0 +1,169 @@
+"""The fused GPU solver against the reference: bit-for-bit on FP64 (golden fixtures made by the
+reference's own code, and the oracle on further cases), by tolerance for the FP32 variant."""
+import ctypes as C
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import armon_gb300 as A
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+FIELDS = ["rho", "umat", "vmat", "Emat", "pmat", "cmat"]
+FUSED = [k for k, v in GOLDEN["cases"].items() if v["case"]["test"] != "Bizarrium"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_solver(case, **kw):
+    s = A.Solver(case, **kw)
+    s.init_test()
+    s.run()
+    p, status = s.state()
+    return s, p, status
+
+
+@pytest.mark.parametrize("name", FUSED)
+def test_fused_solver_matches_reference_bitwise(name):
+    g = GOLDEN["cases"][name]
+    s, p, status = run_solver(A.Case(**g["case"]))
+    with s:
+        assert status == 0
+        assert p.cycle == g["cycles"]
+        assert p.next_cycle_dt == float.fromhex(g["next_cycle_dt"])
+        assert p.current_cycle_dt == float.fromhex(g["current_cycle_dt"])
+        assert p.time == float.fromhex(g["time"])
+        got = {k: sha(A.real_cells(s.params, s.download(k))) for k in FIELDS}
+        bad = [k for k in FIELDS if got[k] != g["hashes"][k]]
+        assert not bad, f"{name}: {bad} differ from the reference"
+        m, e = s.conservation()
+        # the GPU sums in another order: a few ulps of the total
+        assert abs(m - float.fromhex(g["mass"])) <= 1e-13 * abs(m)
+        assert abs(e - float.fromhex(g["energy"])) <= 1e-13 * abs(e)
+        assert s.kernel_launches > 0
+
+
+def _oracle_fields(case):
+    p, st, status, _ = O.run(O.Case(**case.__dict__))
+    assert status == 0
+    return p, {k: O.real_cells(p, st[k]).copy() for k in FIELDS}
+
+
+EXTRA = [
+    # the benchmark's circular Sod at radius 0.2 (squared radius 0.04), a shrunken configuration 2
+    A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=160, ny=96, cfl=0.6,
+           max_cycles=12, max_time=1e9, test_option=0.04),
+    A.Case(test="Sedov", scheme="GAD", projection="euler_2nd", limiter="Superbee", splitting="SequentialSym",
+           nghost=4, nx=75, ny=52, max_cycles=15),
+    A.Case(test="Sod_y", scheme="Godunov", projection="euler_2nd", splitting="Strang", nghost=3, nx=41, ny=67,
+           max_cycles=12, max_time=1.0),
+    A.Case(test="Sod", scheme="GAD", projection="euler", nghost=3, nx=5, ny=4, max_cycles=20, max_time=1.0),
+]
+
+
+@pytest.mark.parametrize("case", EXTRA, ids=lambda c: f"{c.test}-{c.scheme}-{c.projection}-{c.nx}x{c.ny}")
+@pytest.mark.parametrize("seg_len,graph", [(0, 16), (16, 0), (23, 3)])
+def test_fused_solver_matches_oracle_bitwise(case, seg_len, graph):
+    po, ref = _oracle_fields(case)
+    s, p, status = run_solver(case, seg_len=seg_len, cycles_per_graph=graph)
+    with s:
+        assert status == 0 and p.cycle == po.cycle
+        assert p.next_cycle_dt == po.next_cycle_dt and p.time == po.time
+        for k in FIELDS:
+            got = A.real_cells(s.params, s.download(k))
+            assert np.array_equal(got.view(np.int64), ref[k].view(np.int64)), k
+
+
+def test_cycle_limit_and_resume_are_bitwise():
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=64, ny=48,
+                  max_cycles=25, max_time=1e9)
+    po, ref = _oracle_fields(case)
+    s = A.Solver(case, cycles_per_graph=4)
+    with s:
+        s.init_test()
+        s.run(cycle_limit=7)
+        p, _ = s.state()
+        assert p.cycle == 7
+        s.run(cycle_limit=5)
+        s.run()
+        p, status = s.state()
+        assert status == 0 and p.cycle == 25 and p.next_cycle_dt == po.next_cycle_dt
+        for k in FIELDS:
+            assert np.array_equal(A.real_cells(s.params, s.download(k)), ref[k]), k
+
+
+def test_solve_host_end_to_end():
+    """armon_solve_host: host buffers in, host buffers out (the reference-facing call)."""
+    case = A.Case(test="Sod", scheme="Godunov", projection="euler", splitting="SequentialSym", nx=100, ny=100,
+                  cfl=0.6, max_time=0.2, max_cycles=100000)
+    g = GOLDEN["cases"]["cfg1_sod_godunov_100_symsplit"]
+    final, outs = A.solve_host(case)
+    assert final.cycle == g["cycles"] and final.next_cycle_dt == float.fromhex(g["next_cycle_dt"])
+    p = A.make_params(case)
+    for k in ("rho", "umat", "vmat", "Emat", "pmat"):
+        assert sha(A.real_cells(p, outs[k])) == g["hashes"][k], k
+
+
+def test_solve_host_with_uploaded_state_matches_oracle():
+    """A non-test-case initial state given from the host (random smooth perturbation)."""
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=48, ny=40, max_cycles=10,
+                  max_time=1e9)
+    oc = O.Case(**case.__dict__)
+    L = O.lib()
+    po = O.make_params(oc)
+    st = O.OracleState(po)
+    L.o_init_test_p(C.byref(po), C.byref(st.data), 0)
+    rng = np.random.default_rng(7)
+    for k, amp in (("rho", 0.05), ("Emat", 0.1), ("umat", 0.02), ("vmat", 0.02)):
+        st[k][:] = st[k] + amp * rng.standard_normal(st[k].size) * (st[k] != 0 if k in ("rho", "Emat") else 1)
+    inputs = {k: st[k].copy() for k in ("rho", "umat", "vmat", "Emat")}
+    status = C.c_int()
+    L.o_time_loop(C.byref(po), C.byref(st.data), C.byref(status))
+    final, outs = A.solve_host(case, inputs=inputs)
+    assert final.cycle == po.cycle and final.next_cycle_dt == po.next_cycle_dt
+    p = A.make_params(case)
+    for k in ("rho", "umat", "vmat", "Emat", "pmat"):
+        assert np.array_equal(A.real_cells(p, outs[k]), O.real_cells(po, st[k])), k
+
+
+def test_fp32_variant_close_to_fp64_oracle():
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=128, ny=128, cfl=0.6,
+                  max_cycles=40, max_time=1e9, test_option=0.04)
+    po, ref = _oracle_fields(case)
+    s, p, status = run_solver(case, precision=32)
+    with s:
+        assert status == 0 and p.cycle == 40
+        # dt is reduced in FP64 from FP32 fields: same cycle count, dt close
+        assert abs(p.next_cycle_dt - po.next_cycle_dt) <= 1e-5 * po.next_cycle_dt
+        for k in ("rho", "Emat"):
+            got = A.real_cells(s.params, s.download(k))
+            l1 = np.abs(got - ref[k]).sum() / np.abs(ref[k]).sum()
+            assert l1 <= 1e-5, (k, l1)
+        m, e = s.conservation()
+        assert np.isfinite(m) and np.isfinite(e)
+
+
+def test_invalid_dt_is_reported_not_fatal():
+    """A state that gives dt <= 0 stops the loop with ARMON_ERR_INVALID_DT (the reference exits)."""
+    case = A.Case(test="Sod", scheme="GAD", projection="euler_2nd", nghost=5, nx=32, ny=32, max_cycles=10)
+    s = A.Solver(case)
+    with s:
+        s.init_test()
+        E = s.download("Emat")
+        p = s.params
+        g, R = p.nb_ghosts, p.row_length
+        E.reshape(p.col_length, R)[g + 3, g + 3] = np.inf   # c = inf there, so dt_CFL == 0
+        s.upload("Emat", E)
+        s.begin_loop()
+        with pytest.raises(A.ArmonError) as ei:
+            s.run()
+        assert ei.value.code == A.ERR_INVALID_DT
+        _, status = s.state()
+        assert status == 1

@@ -1,0 +1,312 @@
+"""The reference's kernel ABI on the GPU (include/armon_kernels.h), stage by stage: the reference's
+driver sequence (src/armon_2D.cpp:304-386) replayed through the CUDA entry points and compared with
+the reference's own per-stage state (golden hashes of all 16 arrays, ghosts included)."""
+import ctypes as C
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import armon_gb300 as A
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+class DeviceData:
+    """The 16 arrays of src/data.h on the device (torch memory), as labelled armon_views."""
+
+    def __init__(self, n, labelled=True):
+        self.t = {k: torch.zeros(n, dtype=torch.float64, device="cuda") for k in O.ARRAY_NAMES}
+        self.labels = {k: ("Armon_" + k).encode() for k in O.ARRAY_NAMES}
+        self.v = {k: A.View(self.t[k].data_ptr(), n, self.labels[k] if labelled else None) for k in O.ARRAY_NAMES}
+
+    def __getitem__(self, k):
+        return C.byref(self.v[k])
+
+    def host(self, k):
+        torch.cuda.synchronize()
+        return self.t[k].cpu().numpy()
+
+
+def r2(L, dom):
+    r, ir = O.ORange(), O.OInner2D()
+    L.o_domain_iter2D(dom, C.byref(r), C.byref(ir))
+    return A.Range(r.start, r.end), A.InnerRange2D(ir.main_range_start, ir.main_range_step, ir.row_range_start,
+                                                   ir.row_range_length)
+
+
+def r1(L, dom, direct=False):
+    r, ir = O.ORange(), O.OInner1D()
+    (L.o_domain_direct_iter1D if direct else L.o_domain_iter1D)(dom, C.byref(r), C.byref(ir))
+    return A.Range(r.start, r.end), A.InnerRange1D(ir.start, ir.step)
+
+
+class StageDriver:
+    """src/armon_2D.cpp:70-252 on top of the GPU entry points (domains from the oracle)."""
+
+    def __init__(self, p, d):
+        self.p, self.d, self.O, self.K = p, d, O.lib(), A.lib()
+        K = self.K
+        K.dt_CFL.argtypes = [C.c_void_p] * 2 + [C.c_double] * 2 + [C.c_void_p] * 4
+
+    def u(self):
+        return self.d["umat"] if self.p.current_axis == 0 else self.d["vmat"]
+
+    def init_test(self):
+        p, d = self.p, self.d
+        rg, ir = r2(self.O, self.O.o_complete_domain(C.byref(p)))
+        dx, dy = p.domain_size[0] / p.nx, p.domain_size[1] / p.ny
+        topt = p.test_option
+        if p.test == 4 and topt == 0:
+            topt = float(np.hypot(dx, dy) / np.sqrt(2.0))
+        K = self.K
+        K.init_test.argtypes = [C.c_void_p, C.c_void_p] + [C.c_int64] * 4 + [C.c_double] * 4 + [C.c_int64] * 4 + \
+            [C.c_void_p] * 12 + [C.c_int32, C.c_bool, C.c_double]
+        K.init_test(C.byref(rg), C.byref(ir), p.row_length, p.nb_ghosts, p.nx, p.ny, p.domain_size[0],
+                    p.domain_size[1], p.domain_origin[0], p.domain_origin[1], 0, 0, p.nx, p.ny,
+                    d["x"], d["y"], d["rho"], d["Emat"], d["umat"], d["vmat"], d["domain_mask"], d["pmat"],
+                    d["cmat"], d["gmat"], d["ustar"], d["pstar"], p.test, False, topt)
+
+    def update_EOS(self):
+        p, d = self.p, self.d
+        rg, ir = r2(self.O, self.O.o_real_domain(C.byref(p)))
+        if p.test == 3:
+            self.K.bizarrium_EOS(C.byref(rg), C.byref(ir), d["rho"], d["umat"], d["vmat"], d["Emat"], d["pmat"],
+                                 d["cmat"], d["gmat"])
+        else:
+            self.K.perfect_gas_EOS.argtypes = [C.c_void_p, C.c_void_p, C.c_double] + [C.c_void_p] * 7
+            self.K.perfect_gas_EOS(C.byref(rg), C.byref(ir), 1.4, d["rho"], d["Emat"], d["umat"], d["vmat"],
+                                   d["pmat"], d["cmat"], d["gmat"])
+
+    def boundary_conditions(self):
+        p, d = self.p, self.d
+        sides = (0, 1) if p.current_axis == 0 else (2, 3)
+        self.K.boundary_conditions.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_double,
+                                               C.c_double] + [C.c_void_p] * 7
+        for side in sides:
+            disp = C.c_int32()
+            dom = self.O.o_boundary_conditions_domain(C.byref(p), side, C.byref(disp))
+            uf, vf = C.c_double(), C.c_double()
+            self.O.o_boundary_factors(p.test, side, C.byref(uf), C.byref(vf))
+            rg, ir = r1(self.O, dom, direct=True)
+            self.K.boundary_conditions(C.byref(rg), C.byref(ir), p.stencil_width, disp.value, uf.value, vf.value,
+                                       d["rho"], d["umat"], d["vmat"], d["pmat"], d["cmat"], d["gmat"], d["Emat"])
+
+    def numerical_fluxes(self):
+        p, d = self.p, self.d
+        rg, ir = r2(self.O, self.O.o_domain_fluxes(C.byref(p)))
+        if p.scheme == 0:
+            self.K.acoustic.argtypes = [C.c_void_p, C.c_void_p, C.c_int64] + [C.c_void_p] * 6
+            self.K.acoustic(C.byref(rg), C.byref(ir), p.s, d["ustar"], d["pstar"], d["rho"], self.u(), d["pmat"],
+                            d["cmat"])
+        else:
+            self.K.acoustic_GAD.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double] + \
+                [C.c_void_p] * 6 + [C.c_int32]
+            self.K.acoustic_GAD(C.byref(rg), C.byref(ir), p.s, p.cycle_dt, p.dx, d["ustar"], d["pstar"], d["rho"],
+                                self.u(), d["pmat"], d["cmat"], p.limiter)
+
+    def cell_update(self):
+        p, d = self.p, self.d
+        rg, ir = r2(self.O, self.O.o_domain_cell_update(C.byref(p)))
+        self.K.cell_update.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double] + [C.c_void_p] * 5
+        self.K.cell_update(C.byref(rg), C.byref(ir), p.s, p.dx, p.cycle_dt, d["ustar"], d["pstar"], d["rho"],
+                           self.u(), d["Emat"])
+
+    def projection_remap(self):
+        p, d = self.p, self.d
+        rg, ir = r2(self.O, self.O.o_domain_advection(C.byref(p)))
+        w = [d["work_array_1"], d["work_array_2"], d["work_array_3"], d["work_array_4"]]
+        if p.projection == 1:
+            self.K.advection_first_order.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double] + [C.c_void_p] * 9
+            self.K.advection_first_order(C.byref(rg), C.byref(ir), p.s, p.cycle_dt, d["ustar"], d["rho"], d["umat"],
+                                         d["vmat"], d["Emat"], *w)
+        else:
+            self.K.advection_second_order.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double] + \
+                [C.c_void_p] * 9
+            self.K.advection_second_order(C.byref(rg), C.byref(ir), p.s, p.dx, p.cycle_dt, d["ustar"], d["rho"],
+                                          d["umat"], d["vmat"], d["Emat"], *w)
+        rg, ir = r2(self.O, self.O.o_real_domain(C.byref(p)))
+        self.K.euler_projection.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double] + \
+            [C.c_void_p] * 9
+        self.K.euler_projection(C.byref(rg), C.byref(ir), p.s, p.dx, p.cycle_dt, d["ustar"], d["rho"], d["umat"],
+                                d["vmat"], d["Emat"], *w)
+
+    def dt_CFL(self):
+        p, d = self.p, self.d
+        rg, ir = r1(self.O, self.O.o_real_domain(C.byref(p)))
+        dx, dy = p.domain_size[0] / p.nx, p.domain_size[1] / p.ny
+        return self.K.dt_CFL(C.byref(rg), C.byref(ir), dx, dy, d["umat"], d["vmat"], d["cmat"], d["domain_mask"])
+
+    def time_step(self):
+        # src/armon_2D.cpp:212-252
+        p = self.p
+        p.current_cycle_dt = p.next_cycle_dt
+        if p.cst_dt:
+            p.next_cycle_dt = p.Dt
+        elif not p.dt_on_even_cycles or p.cycle % 2 == 0 or p.current_cycle_dt == 0:
+            dt = self.dt_CFL()
+            if not np.isfinite(dt) or dt <= 0:
+                local = dt
+            elif p.current_cycle_dt == 0:
+                local = p.cfl * dt
+            else:
+                a, b = p.cfl * dt, 1.05 * p.current_cycle_dt
+                local = b if b < a else a
+            assert np.isfinite(local) and local > 0
+            p.next_cycle_dt = local
+        else:
+            p.next_cycle_dt = p.current_cycle_dt
+        if p.cycle == 0:
+            p.current_cycle_dt = p.next_cycle_dt
+
+
+def test_stage_kernels_match_reference_stage_by_stage():
+    s = GOLDEN["stages"]
+    p = O.make_params(O.Case(**s["case"]))
+    d = DeviceData(p.nb_cells)
+    drv = StageDriver(p, d)
+    L = O.lib()
+    recs = iter(s["records"])
+
+    def check(tag):
+        r = next(recs)
+        assert r["tag"] == tag
+        bad = [k for k in O.ARRAY_NAMES if sha(d.host(k)) != r["hashes"][k]]
+        assert not bad, f"{tag} cycle {p.cycle} axis {p.current_axis}: {bad}"
+        assert p.current_cycle_dt == float.fromhex(r["current_cycle_dt"])
+        assert p.next_cycle_dt == float.fromhex(r["next_cycle_dt"])
+
+    drv.init_test()
+    check("init_test")
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    drv.update_EOS()
+    check("EOS_init")
+    while p.time < p.max_time and p.cycle < p.max_cycles:
+        drv.time_step()
+        check("time_step")
+        axes, facs = (C.c_int32 * 3)(), (C.c_double * 3)()
+        for k in range(L.o_split_axes(C.byref(p), axes, facs)):
+            L.o_update_axis(C.byref(p), axes[k])
+            p.cycle_dt = p.current_cycle_dt * facs[k]
+            for fn, tag in ((drv.update_EOS, "EOS"), (drv.boundary_conditions, "boundary_conditions"),
+                            (drv.numerical_fluxes, "numerical_fluxes"), (drv.cell_update, "cell_update"),
+                            (drv.projection_remap, "projection_remap")):
+                fn()
+                check(tag)
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+    check("final")
+
+
+@pytest.mark.parametrize("name", ["ref_Sod_circ", "godunov_euler2_33x33", "strang_superbee_37x23",
+                                  "cfg1_sod_godunov_100_symsplit"])
+def test_stage_driver_full_loop_matches_reference(name):
+    g = GOLDEN["cases"][name]
+    p = O.make_params(O.Case(**g["case"]))
+    d = DeviceData(p.nb_cells)
+    drv = StageDriver(p, d)
+    L = O.lib()
+    drv.init_test()
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    drv.update_EOS()
+    while p.time < p.max_time and p.cycle < p.max_cycles:
+        drv.time_step()
+        axes, facs = (C.c_int32 * 3)(), (C.c_double * 3)()
+        for k in range(L.o_split_axes(C.byref(p), axes, facs)):
+            L.o_update_axis(C.byref(p), axes[k])
+            p.cycle_dt = p.current_cycle_dt * facs[k]
+            drv.update_EOS(); drv.boundary_conditions(); drv.numerical_fluxes(); drv.cell_update()
+            drv.projection_remap()
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+    assert p.cycle == g["cycles"] and p.next_cycle_dt == float.fromhex(g["next_cycle_dt"])
+    got = {k: sha(O.real_cells(p, d.host(k))) for k in ("rho", "umat", "vmat", "Emat", "pmat", "cmat")}
+    assert got == g["hashes"]
+    m, e = C.c_double(), C.c_double()
+    rg, ir = r1(L, L.o_real_domain(C.byref(p)))
+    A.lib().conservation_vars.argtypes = [C.c_void_p, C.c_void_p, C.c_double] + [C.c_void_p] * 5
+    A.lib().conservation_vars(C.byref(rg), C.byref(ir), p.dx, d["rho"], d["Emat"], d["domain_mask"], C.byref(m),
+                              C.byref(e))
+    assert abs(m.value - float.fromhex(g["mass"])) <= 1e-13 * abs(m.value)
+    assert abs(e.value - float.fromhex(g["energy"])) <= 1e-13 * abs(e.value)
+
+
+def test_bizarrium_stages_close_to_reference():
+    """bizarrium_EOS uses CUDA's pow: the Bizarrium run agrees with the reference to rounding."""
+    g = GOLDEN["cases"]["ref_Bizarrium"]
+    p = O.make_params(O.Case(**g["case"]))
+    d = DeviceData(p.nb_cells)
+    drv = StageDriver(p, d)
+    L = O.lib()
+    drv.init_test()
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    drv.update_EOS()
+    while p.time < p.max_time and p.cycle < p.max_cycles:
+        drv.time_step()
+        axes, facs = (C.c_int32 * 3)(), (C.c_double * 3)()
+        for k in range(L.o_split_axes(C.byref(p), axes, facs)):
+            L.o_update_axis(C.byref(p), axes[k])
+            p.cycle_dt = p.current_cycle_dt * facs[k]
+            drv.update_EOS(); drv.boundary_conditions(); drv.numerical_fluxes(); drv.cell_update()
+            drv.projection_remap()
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+    assert p.cycle == g["cycles"]
+    assert abs(p.next_cycle_dt - float.fromhex(g["next_cycle_dt"])) <= 1e-9 * p.next_cycle_dt
+    po, st, _, _ = O.run(O.Case(**g["case"]))
+    for k in ("rho", "Emat", "pmat"):
+        a, b = O.real_cells(p, d.host(k)), O.real_cells(po, st[k])
+        assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max(), k
+
+
+def test_border_arrays_roundtrip():
+    """read_border_array / write_border_array (src/kernels/halo_exchange.cpp:39-92) against the oracle."""
+    p = O.make_params(O.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=20, ny=12))
+    n = p.nb_cells
+    rng = np.random.default_rng(3)
+    host = {k: rng.standard_normal(n) for k in O.ARRAY_NAMES}
+    d = DeviceData(n)
+    for k in O.ARRAY_NAMES:
+        d.t[k].copy_(torch.from_numpy(host[k]))
+    nghost, side = 5, p.ny
+    # the left border: nghost columns of the real rows
+    dom = O.ODomain(p.index_start, p.row_length, p.index_start + (p.ny - 1) * p.row_length, 0, 1, nghost - 1)
+    rg, ir = r2(O.lib(), dom)
+    va = torch.zeros(7 * nghost * side, dtype=torch.float64, device="cuda")
+    vv = A.View(va.data_ptr(), va.numel(), b"value_array")
+    K = A.lib()
+    K.read_border_array.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 8
+    K.read_border_array(C.byref(rg), C.byref(ir), side, nghost, d["rho"], d["umat"], d["vmat"], d["pmat"],
+                        d["cmat"], d["gmat"], d["Emat"], C.byref(vv))
+    ref = np.zeros(7 * nghost * side)
+    ors, oir = O.ORange(rg.start, rg.end), O.OInner2D(ir.main_range_start, ir.main_range_step, ir.row_range_start,
+                                                      ir.row_range_length)
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    O.lib().o_read_border_array(ors, oir, side, nghost, ptr(host["rho"]), ptr(host["umat"]), ptr(host["vmat"]),
+                                ptr(host["pmat"]), ptr(host["cmat"]), ptr(host["gmat"]), ptr(host["Emat"]), ptr(ref))
+    torch.cuda.synchronize()
+    assert np.array_equal(va.cpu().numpy(), ref)
+    # write it back, shifted by 3 rows, on both sides
+    va2 = va * 2.0
+    vv2 = A.View(va2.data_ptr(), va2.numel(), b"value_array")
+    K.write_border_array.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 8
+    K.write_border_array(C.byref(rg), C.byref(ir), side, nghost, d["rho"], d["umat"], d["vmat"], d["pmat"],
+                         d["cmat"], d["gmat"], d["Emat"], C.byref(vv2))
+    ref2 = ref * 2.0
+    O.lib().o_write_border_array(ors, oir, side, nghost, ptr(host["rho"]), ptr(host["umat"]), ptr(host["vmat"]),
+                                 ptr(host["pmat"]), ptr(host["cmat"]), ptr(host["gmat"]), ptr(host["Emat"]), ptr(ref2))
+    for k in ("rho", "umat", "vmat", "pmat", "cmat", "gmat", "Emat"):
+        assert np.array_equal(d.host(k), host[k]), k

@@ -36,12 +36,14 @@ WORKLOAD = dict(test="Sod_circ", scheme="GAD", projection="euler_2nd", limiter="
 BYTES_PER_CELL_UPDATE = 64          # read + write rho, u, v, E once per cycle (FP64)
 
 
-def config(nx: int, ny: int, n: int) -> dict:
-    return {"workload": f"Sod_circ {nx}x{ny} FP64, GAD-minmod + euler_2nd, CFL 0.6, radius 0.2, Sequential splitting",
+def config(nx: int, ny: int, n: int, precision: int = 64) -> dict:
+    prec = "FP64" if precision == 64 else "FP32 storage and arithmetic, FP64 dt and conservation sums"
+    esize = 8 if precision == 64 else 4
+    return {"workload": f"Sod_circ {nx}x{ny} {prec}, GAD-minmod + euler_2nd, CFL 0.6, radius 0.2, Sequential splitting",
             "nx": nx, "ny": ny, "nghost": 5, "gamma": 1.4, "scheme": "GAD", "limiter": "Minmod",
             "projection": "euler_2nd", "splitting": "Sequential", "cfl": 0.6, "radius": 0.2,
             "step": "one solver cycle (dt_CFL + X pass + Y pass)",
-            "l2": "inputs larger than L2 (state 4 x %d MB per buffer set)" % ((nx + 10) * (ny + 10) * 8 // 2**20),
+            "l2": "inputs larger than L2 (state: 4 arrays x %d MB per buffer set)" % ((nx + 10) * (ny + 10) * esize // 2**20),
             "parallelism": f"replicas x{n}" if n > 1 else "single domain"}
 
 
@@ -211,8 +213,11 @@ def run_gpu(args) -> None:
     case = A.Case(**WORKLOAD)
     case.nx, case.ny = nx, ny
     case.max_cycles = W + K
-    stream = torch.cuda.current_stream()
-    s = A.Solver(case, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    prec = args.precision
+    # a dedicated stream: the solver launches on it and the CUDA events are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph)
     s.init_test()
     s.enqueue_cycles(W)
     torch.cuda.synchronize()
@@ -253,7 +258,7 @@ def run_gpu(args) -> None:
     case_e2e = A.Case(**WORKLOAD)
     case_e2e.nx, case_e2e.ny = nx, ny
     case_e2e.max_cycles = K
-    se = A.Solver(case_e2e, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph)
     se.init_test()
     outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
             for k in ("rho", "umat", "vmat", "Emat", "pmat")}
@@ -280,22 +285,25 @@ def run_gpu(args) -> None:
     if rank == 0:
         peak, peak_kind = measured_peaks()
         t_launch = ms_max / 1e3 / (K * 2)
-        achieved = BYTES_PER_CELL_UPDATE / 2 * cells / t_launch / 1e9
+        bpc = BYTES_PER_CELL_UPDATE if prec == 64 else BYTES_PER_CELL_UPDATE // 2
+        achieved = bpc / 2 * cells / t_launch / 1e9
         tr = profiled_traffic()
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64", "data": "synthetic", "config": config(nx, ny, world),
+               "dtype": "f64" if prec == 64 else "f32", "data": "synthetic", "config": config(nx, ny, world, prec),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_source": peak_kind,
-                            "traffic": (tr * cells if tr else None),
-                            "kernel": "armon::sweep_kernel<double,1,2,*> (one launch = one axis pass)",
-                            "algorithmic_bytes_per_launch": BYTES_PER_CELL_UPDATE / 2 * cells,
+                            "traffic": (tr * cells if (tr and prec == 64) else None),
+                            "kernel": "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)"
+                                      % ("double" if prec == 64 else "float"),
+                            "algorithmic_bytes_per_launch": bpc / 2 * cells,
                             "note": "FP64 arithmetic bound: see fp64_pipe in profiles/"},
                "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
                        "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,
+                       "host_arrays": "FP64 (converted to the solver's precision inside the call)",
                        "path": "armon_solver_upload x4 (pinned) + begin_loop + run + armon_solver_download x5"},
                "gpu_launches": launches, "clocks": clocks}
-        if world == 1 and not args.no_cpu:
+        if world == 1 and not args.no_cpu and prec == 64:
             out["cpu_baseline"] = cpu_port_throughput(nx, ny, args.cpu_seconds, 200)
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -308,13 +316,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--size", type=int, default=0, help="cells per side (default 4096; 8192 for --precision 32)")
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.size <= 0:
+        args.size = 4096 if args.precision == 64 else 8192
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -121,8 +121,11 @@ def test_solve_host_with_uploaded_state_matches_oracle():
     st = O.OracleState(po)
     L.o_init_test_p(C.byref(po), C.byref(st.data), 0)
     rng = np.random.default_rng(7)
-    for k, amp in (("rho", 0.05), ("Emat", 0.1), ("umat", 0.02), ("vmat", 0.02)):
-        st[k][:] = st[k] + amp * rng.standard_normal(st[k].size) * (st[k] != 0 if k in ("rho", "Emat") else 1)
+    # relative perturbations keep rho and E positive (a NaN state is not bit-portable across CPUs/GPUs)
+    for k, amp in (("rho", 0.05), ("Emat", 0.1)):
+        st[k][:] = st[k] * (1 + amp * rng.uniform(-1, 1, st[k].size))
+    for k in ("umat", "vmat"):
+        st[k][:] = 0.02 * rng.uniform(-1, 1, st[k].size)
     inputs = {k: st[k].copy() for k in ("rho", "umat", "vmat", "Emat")}
     status = C.c_int()
     L.o_time_loop(C.byref(po), C.byref(st.data), C.byref(status))

@@ -32,7 +32,9 @@ UNITS = [
     ("abi_kernels.cu", ["--fmad=false"]),
     ("solver.cu", ["--fmad=false"]),
     ("params.cpp", []),
+    ("armon_2D.cpp", []),
 ]
+CLI_SRC = "main_2D.cpp"
 
 
 def nvcc() -> str:
@@ -84,6 +86,14 @@ def build(clean: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # the command line of the reference, linked against the library
+    cli_obj = _compile(CLI_SRC, [], verbose)
+    if not _newer(CLI, [cli_obj, LIB]):
+        cmd = [nvcc()] + ARCH + ["-o", CLI, cli_obj, "-L" + os.path.dirname(LIB), "-larmon_gb300",
+                                 "-Xlinker", "-rpath=$ORIGIN", "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link of {CLI_SRC} failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -232,13 +232,13 @@ void acoustic_GAD(const Range* range, const InnerRange2D* inner_range, Idx s, fl
                   view* pstar, const view* rho, const view* u, const view* pmat, const view* cmat, Limiter lim)
 {
     guarded("acoustic_GAD", [&] {
-        if (lim < 0 || lim > 2)
-            throw std::out_of_range("Invalid limiter index: " + std::to_string(lim) + ", expected a value between 0 and 2");
+        const int L = static_cast<int>(lim);
+        if (L < 0 || L > 2)
+            throw std::out_of_range("Invalid limiter index: " + std::to_string(L) + ", expected a value between 0 and 2");
         CHECK_LABEL(ustar); CHECK_LABEL(pstar); CHECK_LABEL(rho); CHECK_LABEL(pmat); CHECK_LABEL(cmat);
         const InnerRange2D ir = *inner_range;
         double *ust = ustar->data, *pst = pstar->data;
         const double *rh = rho->data, *uu = u->data, *p = pmat->data, *c = cmat->data;
-        const int L = lim;
         launch_range(range, [=] __device__(int64_t k) {
             // src/kernels/acoustic.cpp:109-148
             int64_t i = scale2d(ir, (uint64_t)k);
@@ -526,8 +526,9 @@ void init_test(const Range* range, const InnerRange2D* inner_range, Idx row_leng
                view* gmat, view* ustar, view* pstar, Test test, bool debug_indexes, flt_t test_option)
 {
     guarded("init_test", [&] {
-        if (test < 0 || test > 4)
-            throw std::out_of_range("Invalid test case index: " + std::to_string(test) +
+        const int test_i = static_cast<int>(test);
+        if (test_i < 0 || test_i > 4)
+            throw std::out_of_range("Invalid test case index: " + std::to_string(test_i) +
                                     ", expected a value between 0 and 4");
         CHECK_LABEL(x); CHECK_LABEL(y); CHECK_LABEL(rho); CHECK_LABEL(Emat); CHECK_LABEL(umat); CHECK_LABEL(vmat);
         CHECK_LABEL(domain_mask); CHECK_LABEL(pmat); CHECK_LABEL(cmat); CHECK_LABEL(gmat); CHECK_LABEL(ustar);
@@ -537,9 +538,9 @@ void init_test(const Range* range, const InnerRange2D* inner_range, Idx row_leng
         a.pos_x = pos_x; a.pos_y = pos_y; a.g_nx = g_nx; a.g_ny = g_ny;
         a.sx = sx; a.sy = sy; a.ox = ox; a.oy = oy;
         a.test_option = test_option;
-        a.test = test;
+        a.test = test_i;
         a.debug_indexes = debug_indexes ? 1 : 0;
-        a.tp = armon::make_test_params(test, test_option);
+        a.tp = armon::make_test_params(test_i, test_option);
         const InnerRange2D ir = *inner_range;
         double *px = x->data, *py = y->data, *r = rho->data, *E = Emat->data, *u = umat->data, *v = vmat->data,
                *m = domain_mask->data, *p = pmat->data, *c = cmat->data, *g = gmat->data, *us = ustar->data,

@@ -248,7 +248,8 @@ void armon_solver_opts_default(armon_solver_opts* o)
     o->materialize_eos = 1;
 }
 
-int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, void* stream, armon_solver** out)
+static int solver_create(const armon_params* p, const armon_solver_opts* opts, double* const* borrowed, void* stream,
+                         armon_solver** out)
 {
     *out = nullptr;
     int rc = check_supported(p);
@@ -274,13 +275,22 @@ int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, vo
         s->own_stream = true;
     }
     size_t bytes = (size_t)p->nb_cells * s->elem;
-    s->owns_arrays = true;
-    for (int k = 0; k < 16; k++) {
-        e = cudaMalloc(&s->arr[k], bytes);
-        if (e != cudaSuccess) {
-            armon_solver_destroy(s);
-            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-            return ARMON_ERR_NOMEM;
+    if (borrowed) {
+        if (s->fp32) { armon_solver_destroy(s); set_error("borrowed arrays are FP64"); return ARMON_ERR_PARAMS; }
+        for (int k = 0; k < 16; k++) {
+            if (!borrowed[k]) { armon_solver_destroy(s); set_error("a borrowed array is NULL"); return ARMON_ERR_PARAMS; }
+            s->arr[k] = borrowed[k];
+        }
+        s->owns_arrays = false;
+    } else {
+        s->owns_arrays = true;
+        for (int k = 0; k < 16; k++) {
+            e = cudaMalloc(&s->arr[k], bytes);
+            if (e != cudaSuccess) {
+                armon_solver_destroy(s);
+                set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+                return ARMON_ERR_NOMEM;
+            }
         }
     }
     e = cudaMalloc(&s->d_state, sizeof(StepState));
@@ -307,6 +317,17 @@ int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, vo
     else { s->a64.state = s->d_state; s->a64.partials = s->d_partials; s->a64.write_eos = s->o.materialize_eos; }
     *out = s;
     return ARMON_OK;
+}
+
+int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, void* stream, armon_solver** out)
+{
+    return solver_create(p, opts, nullptr, stream, out);
+}
+
+int armon_solver_create_with_arrays(const armon_params* p, const armon_solver_opts* opts, double* const arrays[16],
+                                    void* stream, armon_solver** out)
+{
+    return solver_create(p, opts, arrays, stream, out);
 }
 
 void armon_solver_destroy(armon_solver* s)

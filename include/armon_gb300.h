@@ -67,6 +67,11 @@ void armon_params_init(armon_params* p);              /* Params::init, src/param
 int armon_params_check(const armon_params* p);        /* Params::check: 1 = valid, src/parameters.cpp:70-109 */
 int armon_min_ghosts(const armon_params* p);          /* src/parameters.cpp:11-18 */
 int armon_params_sizeof(void);
+/* BC_* sign factors (u_factor, v_factor) of a test case on one side, src/kernels/test_cases.h:36-121 */
+void armon_boundary_factors(int test, int side, double* u_factor, double* v_factor);
+/* TestCase::test_option as the driver passes it to init_test (src/armon_2D.cpp:116-118), with a
+ * non-zero armon_params.test_option taking precedence */
+double armon_test_option(const armon_params* p, double dx, double dy);
 const char* armon_last_error(void);
 int armon_device_count(void);
 
@@ -91,7 +96,18 @@ void armon_solver_opts_default(armon_solver_opts* o);
  * solver creates).  The solver keeps a copy of `p`. */
 int armon_solver_create(const armon_params* p, const armon_solver_opts* opts, void* stream,
                         armon_solver** out);
+/* The same on 16 caller-owned FP64 device arrays of nb_cells values (the reference's DataHolder
+ * order: x y rho umat vmat Emat pmat cmat gmat ustar pstar work_array_1..4 domain_mask).  The
+ * fused path uses the four work arrays as its second state buffer; after armon_solver_run returns,
+ * rho/umat/vmat/Emat/pmat/cmat/gmat hold the state as the reference's time loop leaves them.
+ * The arrays are not freed by armon_solver_destroy. */
+int armon_solver_create_with_arrays(const armon_params* p, const armon_solver_opts* opts, double* const arrays[16],
+                                    void* stream, armon_solver** out);
 void armon_solver_destroy(armon_solver* s);
+
+/* Restarts the time loop on the current arrays (the start of time_loop, src/armon_2D.cpp:327-346:
+ * cycle = 0, time = 0, update_EOS, and the first dt_CFL).  Call after uploading a new state. */
+int armon_solver_begin_loop(armon_solver* s);
 
 /* init_test on the device (src/armon_2D.cpp:112-127) followed by the EOS and the first dt
  * reduction of time_loop (src/armon_2D.cpp:327-346). */

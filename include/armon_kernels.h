@@ -32,8 +32,16 @@ extern "C" {
 typedef double flt_t;
 typedef int64_t Idx;
 typedef uint64_t UIdx;
+#ifdef __cplusplus
+}
+/* C++ callers get the reference's scoped enums (same 32-bit representation as the C typedefs). */
+enum class Limiter : int32_t { None = 0, Minmod = 1, Superbee = 2 };                          /* src/kernels/limiters.h:8-12 */
+enum class Test : int32_t { Sod = 0, Sod_y = 1, Sod_circ = 2, Bizarrium = 3, Sedov = 4 };   /* src/kernels/test_cases.h:8-14 */
+extern "C" {
+#else
 typedef int32_t Limiter;   /* src/kernels/limiters.h:8-12: None 0, Minmod 1, Superbee 2 */
 typedef int32_t Test;      /* src/kernels/test_cases.h:8-14: Sod 0 .. Sedov 4 */
+#endif
 
 /* src/kernels/indexing.h:28-33 */
 typedef struct Range { Idx start; Idx end; } Range;

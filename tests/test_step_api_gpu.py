@@ -118,7 +118,9 @@ def test_cli_bizarrium_uses_stage_kernels(tmp_path):
 
 @pytest.mark.gpu
 def test_cli_verbose_conservation_lines(tmp_path):
-    r = run_cli(["-t", "Sod", "-s", "GAD", "--projection", "euler_2nd", "--nghost", "5", "--cells", "64,32",
+    # a square domain: the reference's conservation_vars uses ds = dx*dx of the current axis
+    # (src/kernels/reductions.cpp:38), so on dx != dy its own |dM| line jumps by (dy/dx)^2
+    r = run_cli(["-t", "Sod", "-s", "GAD", "--projection", "euler_2nd", "--nghost", "5", "--cells", "64,64",
                  "--cycle", "12", "--verbose", "1"], tmp_path)
     assert r.returncode == 0, r.stderr
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("Cycle =")]

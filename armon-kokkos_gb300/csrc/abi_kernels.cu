@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -197,6 +198,70 @@ __global__ void sum2_final_kernel(const double* partials, int n, double* out)
 }
 
 constexpr int kReduceBlocks = 152 * 4;
+
+// ---- dt_CFL without device allocation --------------------------------------------------------
+// One partial minimum per tile of kNoAllocTile indices, in a fixed array that lives in the module
+// (every GPU that loads the library holds it until the process exits), plus one slot for the
+// result.  256 KB: ranges of up to kNoAllocMaxTiles * kNoAllocTile = 134,217,728 indices.
+constexpr int kNoAllocTile = 4096;
+constexpr int kNoAllocMaxTiles = 32768;
+static __device__ __align__(256) double g_dt_no_alloc_scratch[kNoAllocMaxTiles + 1];
+
+__global__ void dt_tile_kernel(int64_t start, int64_t end, InnerRange1D ir, double dx, double dy, const double* umat,
+                               const double* vmat, const double* cmat, const double* mask, double* partials)
+{
+    // the same per-index formula as dt_partial_kernel, one tile of kNoAllocTile indices per block
+    __shared__ double red[256];
+    double acc = DBL_MAX;
+    const int64_t t0 = start + (int64_t)blockIdx.x * kNoAllocTile;
+    const int64_t t1 = min(end, t0 + kNoAllocTile);
+    for (int64_t k = t0 + threadIdx.x; k < t1; k += blockDim.x) {
+        int64_t i = scale1d(ir, (uint64_t)k);
+        double max_cx = kmax(fabs(umat[i] + cmat[i]), fabs(umat[i] - cmat[i])) * mask[i];
+        double max_cy = kmax(fabs(vmat[i] + cmat[i]), fabs(vmat[i] - cmat[i])) * mask[i];
+        acc = kmin(acc, kmin(dx / max_cx, dy / max_cy));
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) { double o = red[threadIdx.x + w]; if (o < red[threadIdx.x]) red[threadIdx.x] = o; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = red[0];
+}
+
+__global__ void min_tiles_kernel(const double* partials, int n, double* out)
+{
+    __shared__ double red[1024];
+    double acc = DBL_MAX;
+    for (int b = threadIdx.x; b < n; b += blockDim.x)
+        if (partials[b] < acc) acc = partials[b];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) { double o = red[threadIdx.x + w]; if (o < red[threadIdx.x]) red[threadIdx.x] = o; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
+// Device address of g_dt_no_alloc_scratch, resolved once per device with that device current.
+// In host code the symbol itself is only a host-side stand-in for the array.
+double* no_alloc_scratch_address()
+{
+    static std::mutex mu;
+    static double* addr[64] = {};
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range for the static scratch table");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        check_cuda(cudaGetSymbolAddress(&p, g_dt_no_alloc_scratch), "cudaGetSymbolAddress");
+        addr[dev] = static_cast<double*>(p);
+    }
+    return addr[dev];
+}
 
 }  // namespace
 
@@ -568,6 +633,33 @@ flt_t dt_CFL(const Range* range, const InnerRange1D* inner_range, flt_t dx, flt_
         check_cuda(cudaMemcpyAsync(&result, buf + kReduceBlocks, sizeof(double), cudaMemcpyDeviceToHost, g_stream),
                    "dt_CFL copy");
         check_cuda(cudaStreamSynchronize(g_stream), "dt_CFL sync");
+    });
+    return result;
+}
+
+flt_t dt_CFL_no_alloc(const Range* range, const InnerRange1D* inner_range, flt_t dx, flt_t dy, const view* umat,
+                      const view* vmat, const view* cmat, const mask_view* domain_mask)
+{
+    // dt_CFL for callers that may not allocate device memory: the per-tile partial minima go to
+    // g_dt_no_alloc_scratch instead of a cudaMalloc'd buffer.  Nothing here allocates.
+    double result = DBL_MAX;
+    guarded("dt_CFL_no_alloc", [&] {
+        CHECK_LABEL(umat); CHECK_LABEL(vmat); CHECK_LABEL(cmat); CHECK_LABEL(domain_mask);
+        int64_t n = range->end - range->start;
+        if (n <= 0) { result = DBL_MAX; return; }
+        int64_t tiles = (n + kNoAllocTile - 1) / kNoAllocTile;
+        if (tiles > kNoAllocMaxTiles)
+            throw std::out_of_range("range of " + std::to_string(n) + " indices exceeds the static scratch limit of " +
+                                    std::to_string((int64_t)kNoAllocMaxTiles * kNoAllocTile) +
+                                    " indices; use dt_CFL");
+        double* scratch_dev = no_alloc_scratch_address();
+        dt_tile_kernel<<<(int)tiles, 256, 0, g_stream>>>(range->start, range->end, *inner_range, dx, dy, umat->data,
+                                                         vmat->data, cmat->data, domain_mask->data, scratch_dev);
+        min_tiles_kernel<<<1, 1024, 0, g_stream>>>(scratch_dev, (int)tiles, scratch_dev + kNoAllocMaxTiles);
+        check_cuda(cudaGetLastError(), "dt_CFL_no_alloc launch");
+        check_cuda(cudaMemcpyAsync(&result, scratch_dev + kNoAllocMaxTiles, sizeof(double), cudaMemcpyDeviceToHost,
+                                   g_stream), "dt_CFL_no_alloc copy");
+        check_cuda(cudaStreamSynchronize(g_stream), "dt_CFL_no_alloc sync");
     });
     return result;
 }

@@ -142,6 +142,22 @@ void init_test(const Range* range, const InnerRange2D* inner_range,
 flt_t dt_CFL(const Range* range, const InnerRange1D* inner_range, flt_t dx, flt_t dy,
              const view* umat, const view* vmat, const view* cmat, const mask_view* domain_mask);
 
+/* No counterpart in the reference.  dt_CFL for callers that may not allocate device memory after
+ * start-up: hosts that hand the whole device to their own memory pool (a Julia or Kokkos runtime
+ * that reserved it), or time-critical loops that cannot afford cudaMalloc's device-wide
+ * synchronisation.  Same arguments and result as dt_CFL, which allocates its reduction scratch on
+ * first use; this variant keeps its scratch in a fixed 256 KB array inside the library's device
+ * module instead, so it calls no cudaMalloc, cudaFree or allocating routine.
+ *  - Limit: ranges of at most 134,217,728 indices (32768 tiles of 4096); a longer range goes to
+ *    raise_exception_handler with an out_of_range message.
+ *  - The first call on each device resolves the array's device address (cudaGetSymbolAddress with
+ *    that device current); make that first call before any stream capture.
+ *  - Every call shares the one array (it keeps the last call's partials; each call overwrites all
+ *    it reads), so calls that overlap on the GPU race: issue them on one stream.
+ *  - Every GPU that loads the library holds the array until the process exits. */
+flt_t dt_CFL_no_alloc(const Range* range, const InnerRange1D* inner_range, flt_t dx, flt_t dy,
+                      const view* umat, const view* vmat, const view* cmat, const mask_view* domain_mask);
+
 /* src/kernels/kernels.h:83-86 (blocking; the sums are written to host memory) */
 void conservation_vars(const Range* range, const InnerRange1D* inner_range, flt_t dx,
                        const view* rho, const view* Emat, const mask_view* domain_mask,

@@ -52,6 +52,11 @@ class SolverOpts(C.Structure):
                 ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
+class BatchOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("block_lines", C.c_int32),
+                ("seg_len", C.c_int32), ("memory_budget", C.c_int64)]
+
+
 class Range(C.Structure):
     _fields_ = [("start", C.c_int64), ("end", C.c_int64)]
 
@@ -104,6 +109,27 @@ def lib() -> C.CDLL:
     L.armon_solver_kernel_launches.argtypes = [S]
     L.armon_solver_kernel_launches.restype = C.c_int64
     L.armon_solve_host.argtypes = [P, C.POINTER(SolverOpts), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), P]
+    B = C.c_void_p
+    L.armon_batch_opts_default.argtypes = [C.POINTER(BatchOpts)]
+    L.armon_batch_create.argtypes = [C.POINTER(BatchOpts), C.c_void_p, C.POINTER(C.c_void_p)]
+    L.armon_batch_destroy.argtypes = [B]
+    L.armon_batch_destroy.restype = None
+    L.armon_batch_domain_bytes.argtypes = [P, C.c_int32]
+    L.armon_batch_domain_bytes.restype = C.c_int64
+    L.armon_batch_add.argtypes = [B, P, C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]
+    L.armon_batch_set_seg_len.argtypes = [B, C.c_int32, C.c_int32]
+    L.armon_batch_enqueue_cycles.argtypes = [B, C.c_int32]
+    L.armon_batch_run.argtypes = [B, C.c_int32, C.POINTER(C.c_int32)]
+    L.armon_batch_poll.argtypes = [B, C.POINTER(C.c_int32)]
+    L.armon_batch_domain_state.argtypes = [B, C.c_int32, P, C.POINTER(C.c_int32)]
+    L.armon_batch_domain_done.argtypes = [B, C.c_int32]
+    L.armon_batch_download.argtypes = [B, C.c_int32, C.c_int, C.c_void_p]
+    L.armon_batch_remove.argtypes = [B, C.c_int32]
+    L.armon_batch_size.argtypes = [B]
+    L.armon_batch_bytes_in_use.argtypes = [B]
+    L.armon_batch_bytes_in_use.restype = C.c_int64
+    L.armon_batch_kernel_launches.argtypes = [B]
+    L.armon_batch_kernel_launches.restype = C.c_int64
     L.dt_CFL.restype = C.c_double
     L.idx_size.restype = C.c_int
     L.is_uidx_signed.restype = C.c_bool
@@ -264,3 +290,99 @@ def solve_host(case: Case | Params, inputs: dict[str, np.ndarray] | None = None,
     final = Params()
     check(L.armon_solve_host(C.byref(p), C.byref(o), ins if inputs else None, outp, C.byref(final)))
     return final, outs
+
+
+class Batch:
+    """Many independent domains advanced together (armon_batch_* of include/armon_gb300.h)."""
+
+    def __init__(self, precision: int = 64, stream: int | None = None, cycles_per_graph: int = 8,
+                 block_lines: int = 128, seg_len: int = 0, memory_budget: int = 0):
+        L = lib()
+        o = BatchOpts()
+        L.armon_batch_opts_default(C.byref(o))
+        o.precision, o.cycles_per_graph, o.block_lines = precision, cycles_per_graph, block_lines
+        o.seg_len, o.memory_budget = seg_len, memory_budget
+        h = C.c_void_p()
+        check(L.armon_batch_create(C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.params: dict[int, Params] = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().armon_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add(self, params: Params | Case, init: dict[str, np.ndarray] | None = None) -> int:
+        p = make_params(params) if isinstance(params, Case) else params
+        arr = None
+        keep = []
+        if init is not None:
+            arr = (C.c_void_p * 4)()
+            for k, name in enumerate(("rho", "umat", "vmat", "Emat")):
+                a = np.ascontiguousarray(init[name], dtype=np.float64)
+                assert a.size == p.nb_cells
+                keep.append(a)
+                arr[k] = a.ctypes.data
+        i = C.c_int32()
+        check(lib().armon_batch_add(self._h, C.byref(p), arr, C.byref(i)))
+        self.params[i.value] = p
+        return i.value
+
+    def set_seg_len(self, i: int, seg_len: int) -> None:
+        check(lib().armon_batch_set_seg_len(self._h, i, seg_len))
+
+    def enqueue_cycles(self, n: int) -> None:
+        check(lib().armon_batch_enqueue_cycles(self._h, n))
+
+    def run(self, cycle_limit: int = 0) -> int:
+        r = C.c_int32()
+        check(lib().armon_batch_run(self._h, cycle_limit, C.byref(r)))
+        return r.value
+
+    def poll(self) -> int:
+        r = C.c_int32()
+        check(lib().armon_batch_poll(self._h, C.byref(r)))
+        return r.value
+
+    def state(self, i: int) -> tuple[Params, int]:
+        p = Params()
+        st = C.c_int32()
+        check(lib().armon_batch_domain_state(self._h, i, C.byref(p), C.byref(st)))
+        return p, st.value
+
+    def done(self, i: int) -> bool:
+        return lib().armon_batch_domain_done(self._h, i) == 1
+
+    def download(self, i: int, name: str) -> np.ndarray:
+        a = np.empty(self.params[i].nb_cells, dtype=np.float64)
+        check(lib().armon_batch_download(self._h, i, ARRAYS.index(name), a.ctypes.data))
+        return a
+
+    def remove(self, i: int) -> None:
+        check(lib().armon_batch_remove(self._h, i))
+        self.params.pop(i, None)
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(lib().armon_batch_bytes_in_use(self._h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().armon_batch_kernel_launches(self._h))
+
+
+def domain_bytes(params: Params, precision: int = 64) -> int:
+    return int(lib().armon_batch_domain_bytes(C.byref(params), precision))

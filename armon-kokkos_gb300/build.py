@@ -31,6 +31,7 @@ UNITS = [
     ("sweep_f32.cu", ["--fmad=true"]),
     ("abi_kernels.cu", ["--fmad=false"]),
     ("solver.cu", ["--fmad=false"]),
+    ("batch.cu", ["--fmad=false"]),
     ("params.cpp", []),
     ("armon_2D.cpp", []),
 ]

@@ -1,0 +1,480 @@
+// batch.cu -- many independent domains advanced together (include/armon_gb300.h, armon_batch_*).
+//
+// Every domain keeps its own state (two buffer sets, p/c/g, dt partials) in one allocation from
+// the batch's stream-ordered memory pool, and its own 48-byte step state in a slot of a device
+// array.  A pass over the batch is one launch of sweep_batch_kernel: the launch table lists the
+// running domains and the first grid block of each (enough blocks for its larger axis), so one
+// launch covers every domain, each with its own dt, time and cycle.  The table is rebuilt when
+// domains join or finish; cycles are captured in a CUDA graph per table.  The host reads all
+// step states back with one copy per graph batch.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "armon_gb300.h"
+#include "host_common.h"
+#include "launch.h"
+#include "solver_common.h"
+
+using namespace armon;
+
+namespace {
+
+constexpr int kMaxDomains = 8192;
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+struct Dom {
+    bool used = false;
+    bool done = false;
+    armon_params p{};
+    void* chunk = nullptr;
+    int64_t bytes = 0;
+    void* arr[11] = {};           // set 0 (rho umat vmat Emat), set 1 (same), pmat cmat gmat
+    double* partials = nullptr;
+    int64_t npartials = 0;        // pairs
+    int seg_len = 0;
+};
+
+int64_t partial_pairs(const armon_params& p, int block)
+{
+    // an upper bound of the blocks either axis may use (segments of at least 16 cells), and the
+    // grid of the EOS + first dt kernel
+    int64_t bx = (int64_t)std::max(1, (p.ny + block - 1) / block) * std::max(1, p.nx / 16 + 1);
+    int64_t by = (int64_t)std::max(1, (p.nx + block - 1) / block) * std::max(1, p.ny / 16 + 1);
+    return std::max<int64_t>(std::max(bx, by), 152 * 4);
+}
+
+}  // namespace
+
+struct armon_batch {
+    armon_batch_opts o{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaMemPool_t pool = nullptr;
+    int sm_count = 152;
+    bool fp32 = false;
+    size_t elem = 8;
+    int scheme = -1, proj = -1, splitting = -1, npass = 2;
+    std::vector<Dom> doms;
+    StepState* d_states = nullptr;
+    StepState* h_states = nullptr;
+    void* d_args = nullptr;
+    int* d_offsets = nullptr;
+    std::vector<int> table;
+    int total_blocks = 0;
+    bool dirty = true;
+    cudaGraphExec_t graph = nullptr;
+    int64_t bytes = 0;
+    int64_t launches = 0;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? ARMON_ERR_NOMEM : ARMON_ERR_CUDA;
+}
+
+#define CUDA_TRY(expr)                                            \
+    do {                                                          \
+        cudaError_t e_ = (expr);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);       \
+    } while (0)
+
+template <class T>
+DomainBuffers<T> buffers(const Dom& d)
+{
+    T* const* a = reinterpret_cast<T* const*>(d.arr);
+    return DomainBuffers<T>{{{a[0], a[1], a[2], a[3]}, {a[4], a[5], a[6], a[7]}}, a[8], a[9], a[10]};
+}
+
+template <class T>
+int rebuild_t(armon_batch* b)
+{
+    b->table.clear();
+    for (int i = 0; i < (int)b->doms.size(); i++)
+        if (b->doms[i].used && !b->doms[i].done) b->table.push_back(i);
+    std::vector<SweepArgs<T>> args(b->table.size());
+    std::vector<int> offsets(b->table.size() + 1, 0);
+    for (size_t k = 0; k < b->table.size(); k++) {
+        Dom& d = b->doms[b->table[k]];
+        int forced = d.seg_len > 0 ? d.seg_len : b->o.seg_len;
+        int nb = make_sweep_args<T>(d.p, b->npass, b->o.block_lines, b->sm_count, forced, buffers<T>(d),
+                                    b->d_states + b->table[k], d.partials, 1, args[k]);
+        if (nb > d.npartials) { set_error("domain needs more partial slots than allotted"); return ARMON_ERR_STATE; }
+        offsets[k + 1] = offsets[k] + nb;
+    }
+    b->total_blocks = offsets.back();
+    if (!b->table.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(SweepArgs<T>), cudaMemcpyHostToDevice,
+                                 b->stream));
+        CUDA_TRY(cudaMemcpyAsync(b->d_offsets, offsets.data(), offsets.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                 b->stream));
+        CUDA_TRY(cudaStreamSynchronize(b->stream));   // the host vectors go out of scope
+    }
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->dirty = false;
+    return ARMON_OK;
+}
+
+int rebuild(armon_batch* b) { return b->fp32 ? rebuild_t<float>(b) : rebuild_t<double>(b); }
+
+int enqueue_direct(armon_batch* b, int n)
+{
+    const int nd = (int)b->table.size();
+    for (int c = 0; c < n; c++) {
+        for (int k = 0; k < b->npass; k++) {
+            bool last = k == b->npass - 1;
+            cudaError_t e = b->fp32
+                ? launch_sweep_batch((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                                     b->scheme, b->proj, last, b->o.block_lines, b->stream)
+                : launch_sweep_batch((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                                     b->scheme, b->proj, last, b->o.block_lines, b->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "batch sweep launch");
+            b->launches++;
+        }
+    }
+    return ARMON_OK;
+}
+
+int enqueue(armon_batch* b, int n)
+{
+    if (b->dirty) {
+        int rc = rebuild(b);
+        if (rc != ARMON_OK) return rc;
+    }
+    if (b->table.empty() || n <= 0) return ARMON_OK;
+    const int gc = b->o.cycles_per_graph;
+    if (gc > 0 && n >= gc) {
+        if (!b->graph) {
+            cudaGraph_t g = nullptr;
+            int64_t saved = b->launches;
+            CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue_direct(b, gc);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            b->launches = saved;
+            if (rc != ARMON_OK) { if (g) cudaGraphDestroy(g); return rc; }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { b->graph = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
+        }
+        while (n >= gc) {
+            CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+            b->launches += (int64_t)gc * b->npass;
+            n -= gc;
+        }
+    }
+    return enqueue_direct(b, n);
+}
+
+int max_slot(const armon_batch* b)
+{
+    int m = 0;
+    for (int i = 0; i < (int)b->doms.size(); i++)
+        if (b->doms[i].used) m = i + 1;
+    return m;
+}
+
+bool loop_running(const Dom& d, const StepState& st)
+{
+    return st.status == STATUS_RUNNING && st.time < d.p.max_time && st.cycle < d.p.max_cycles;
+}
+
+int current_set(const armon_batch* b, int id)
+{
+    const StepState& st = b->h_states[id];
+    return (int)(((int64_t)st.cycle * b->npass + st.buf_base) & 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+void armon_batch_opts_default(armon_batch_opts* o)
+{
+    std::memset(o, 0, sizeof(*o));
+    o->precision = 64;
+    o->cycles_per_graph = 8;
+    o->block_lines = 128;
+}
+
+int64_t armon_batch_domain_bytes(const armon_params* p, int32_t precision)
+{
+    size_t elem = precision == 32 ? 4 : 8;
+    return (int64_t)(11 * align256((size_t)p->nb_cells * elem) + align256(16 * (size_t)partial_pairs(*p, 32)));
+}
+
+int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch** out)
+{
+    *out = nullptr;
+    armon_batch* b = new armon_batch();
+    if (opts) b->o = *opts; else armon_batch_opts_default(&b->o);
+    if (b->o.precision != 32 && b->o.precision != 64) { delete b; set_error("precision must be 32 or 64"); return ARMON_ERR_PARAMS; }
+    if (b->o.block_lines <= 0) b->o.block_lines = 128;
+    if (b->o.block_lines % 32 != 0 || b->o.block_lines > 128) {
+        delete b;
+        set_error("block_lines must be a multiple of 32, at most 128");
+        return ARMON_ERR_PARAMS;
+    }
+    b->fp32 = b->o.precision == 32;
+    b->elem = b->fp32 ? 4 : 8;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaSuccess;
+    if (stream) {
+        b->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        b->own_stream = e == cudaSuccess;
+    }
+    if (e == cudaSuccess) {
+        // a pool of its own that keeps freed memory for the next domain
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        e = cudaMemPoolCreate(&b->pool, &props);
+        if (e == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            e = cudaMemPoolSetAttribute(b->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(StepState) * kMaxDomains);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_states, sizeof(StepState) * kMaxDomains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_args, sizeof(SweepArgs<double>) * kMaxDomains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_offsets, sizeof(int) * (kMaxDomains + 1));
+    if (e != cudaSuccess) {
+        armon_batch_destroy(b);
+        return cuda_fail(e, "batch allocation");
+    }
+    std::memset(b->h_states, 0, sizeof(StepState) * kMaxDomains);
+    *out = b;
+    return ARMON_OK;
+}
+
+void armon_batch_destroy(armon_batch* b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& d : b->doms)
+        if (d.used && d.chunk) cudaFreeAsync(d.chunk, b->stream);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->pool) cudaMemPoolDestroy(b->pool);
+    if (b->d_states) cudaFree(b->d_states);
+    if (b->h_states) cudaFreeHost(b->h_states);
+    if (b->d_args) cudaFree(b->d_args);
+    if (b->d_offsets) cudaFree(b->d_offsets);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int armon_batch_add(armon_batch* b, const armon_params* p, const double* const init[4], int32_t* id)
+{
+    *id = -1;
+    int rc = check_supported(p);
+    if (rc != ARMON_OK) return rc;
+    if (b->scheme < 0) {
+        b->scheme = p->scheme;
+        b->proj = p->projection;
+        b->splitting = p->axis_splitting;
+        b->npass = passes_per_cycle(p->axis_splitting);
+    } else if (b->scheme != p->scheme || b->proj != p->projection || b->splitting != p->axis_splitting) {
+        set_error("all domains of a batch share scheme, projection and axis splitting");
+        return ARMON_ERR_PARAMS;
+    }
+    int64_t need = armon_batch_domain_bytes(p, b->o.precision);
+    if (b->o.memory_budget > 0 && b->bytes + need > b->o.memory_budget) {
+        set_error("the batch's memory budget would be exceeded");
+        return ARMON_ERR_NOMEM;
+    }
+    int slot = -1;
+    for (int i = 0; i < (int)b->doms.size(); i++)
+        if (!b->doms[i].used) { slot = i; break; }
+    if (slot < 0) {
+        if ((int)b->doms.size() >= kMaxDomains) { set_error("too many domains in one batch"); return ARMON_ERR_PARAMS; }
+        b->doms.emplace_back();
+        slot = (int)b->doms.size() - 1;
+    }
+    Dom d;
+    d.p = *p;
+    d.bytes = need;
+    cudaError_t e = cudaMallocFromPoolAsync(&d.chunk, (size_t)need, b->pool, b->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocFromPoolAsync");
+    char* base = (char*)d.chunk;
+    size_t arr_bytes = align256((size_t)p->nb_cells * b->elem);
+    for (int k = 0; k < 11; k++) d.arr[k] = base + k * arr_bytes;
+    d.partials = (double*)(base + 11 * arr_bytes);
+    d.npartials = partial_pairs(*p, 32);
+    b->doms[slot] = d;
+    b->doms[slot].used = true;
+    b->bytes += need;
+    Dom& dd = b->doms[slot];
+
+    // init_test on the device (ghosts, p = 0, c = 1 where the pass never writes), then the host state
+    InitArgs a{};
+    a.row_length = p->row_length; a.nb_ghosts = p->nb_ghosts; a.nx = p->nx; a.ny = p->ny;
+    a.pos_x = 0; a.pos_y = 0; a.g_nx = p->nx; a.g_ny = p->ny;
+    a.sx = p->domain_size[0]; a.sy = p->domain_size[1]; a.ox = p->domain_origin[0]; a.oy = p->domain_origin[1];
+    double dx = p->domain_size[0] / double(p->nx), dy = p->domain_size[1] / double(p->ny);
+    a.test_option = armon_test_option(p, dx, dy);
+    a.test = p->test;
+    a.tp = make_test_params(p->test, a.test_option);
+    InitPtrs ip{nullptr, nullptr, dd.arr[0], dd.arr[3], dd.arr[1], dd.arr[2], nullptr, dd.arr[8], dd.arr[9], dd.arr[10],
+                nullptr, nullptr};
+    CUDA_TRY(launch_init(a, p->nb_cells, ip, b->fp32, b->stream));
+    b->launches++;
+    if (init) {
+        // rho umat vmat Emat of set 0
+        for (int k = 0; k < 4; k++) {
+            if (!init[k]) continue;
+            if (!b->fp32) {
+                CUDA_TRY(cudaMemcpyAsync(dd.arr[k], init[k], (size_t)p->nb_cells * 8, cudaMemcpyHostToDevice, b->stream));
+            } else {
+                std::vector<float> f(init[k], init[k] + p->nb_cells);
+                CUDA_TRY(cudaMemcpyAsync(dd.arr[k], f.data(), (size_t)p->nb_cells * 4, cudaMemcpyHostToDevice, b->stream));
+                CUDA_TRY(cudaStreamSynchronize(b->stream));
+            }
+        }
+    }
+    for (int k = 0; k < 4; k++)
+        CUDA_TRY(cudaMemcpyAsync(dd.arr[4 + k], dd.arr[k], arr_bytes, cudaMemcpyDeviceToDevice, b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_states + slot, 0, sizeof(StepState), b->stream));
+    BeginArgs ba{};
+    ba.nx = p->nx; ba.ny = p->ny;
+    ba.origin = (int64_t)p->nb_ghosts * p->row_length + p->nb_ghosts;
+    ba.row_length = p->row_length;
+    ba.gamma = 1.4;
+    ba.rho = dd.arr[0]; ba.umat = dd.arr[1]; ba.vmat = dd.arr[2]; ba.Emat = dd.arr[3];
+    ba.pmat = dd.arr[8]; ba.cmat = dd.arr[9]; ba.gmat = dd.arr[10];
+    ba.state = b->d_states + slot;
+    ba.cfg = make_step_config(*p);
+    ba.partials = dd.partials;
+    ba.buf_base = 0;
+    CUDA_TRY(launch_begin(ba, b->fp32, 152 * 4, b->stream));
+    b->launches++;
+    std::memset(&b->h_states[slot], 0, sizeof(StepState));
+    b->dirty = true;
+    *id = slot;
+    return ARMON_OK;
+}
+
+int armon_batch_set_seg_len(armon_batch* b, int32_t id, int32_t seg_len)
+{
+    if (id < 0 || id >= (int)b->doms.size() || !b->doms[id].used) { set_error("unknown domain"); return ARMON_ERR_PARAMS; }
+    b->doms[id].seg_len = seg_len;
+    b->dirty = true;
+    return ARMON_OK;
+}
+
+int armon_batch_enqueue_cycles(armon_batch* b, int32_t n) { return enqueue(b, n); }
+
+int armon_batch_poll(armon_batch* b, int32_t* running)
+{
+    int m = max_slot(b);
+    if (m > 0) {
+        CUDA_TRY(cudaMemcpyAsync(b->h_states, b->d_states, sizeof(StepState) * m, cudaMemcpyDeviceToHost, b->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int run = 0;
+    for (int i = 0; i < m; i++) {
+        Dom& d = b->doms[i];
+        if (!d.used) continue;
+        bool r = loop_running(d, b->h_states[i]);
+        if (r) run++;
+        if (!r && !d.done) {
+            d.done = true;
+            b->dirty = true;   // drop it from the launch table
+        }
+    }
+    if (running) *running = run;
+    return ARMON_OK;
+}
+
+int armon_batch_run(armon_batch* b, int32_t cycle_limit, int32_t* running)
+{
+    int issued = 0, run = 0;
+    for (;;) {
+        int rc = armon_batch_poll(b, &run);
+        if (rc != ARMON_OK) return rc;
+        if (run == 0 || (cycle_limit > 0 && issued >= cycle_limit)) break;
+        int n = b->o.cycles_per_graph > 0 ? b->o.cycles_per_graph : 8;
+        if (cycle_limit > 0) n = std::min(n, cycle_limit - issued);
+        rc = enqueue(b, n);
+        if (rc != ARMON_OK) return rc;
+        issued += n;
+    }
+    if (running) *running = run;
+    return ARMON_OK;
+}
+
+int armon_batch_domain_state(armon_batch* b, int32_t id, armon_params* p, int32_t* status)
+{
+    if (id < 0 || id >= (int)b->doms.size() || !b->doms[id].used) { set_error("unknown domain"); return ARMON_ERR_PARAMS; }
+    const StepState& st = b->h_states[id];
+    *p = b->doms[id].p;
+    p->cycle = st.cycle;
+    p->time = st.time;
+    p->current_cycle_dt = st.current_dt;
+    p->next_cycle_dt = st.next_dt;
+    if (status) *status = st.status;
+    return ARMON_OK;
+}
+
+int armon_batch_domain_done(armon_batch* b, int32_t id)
+{
+    if (id < 0 || id >= (int)b->doms.size() || !b->doms[id].used) return -1;
+    return b->doms[id].done ? 1 : 0;
+}
+
+int armon_batch_download(armon_batch* b, int32_t id, int which, double* host)
+{
+    if (id < 0 || id >= (int)b->doms.size() || !b->doms[id].used) { set_error("unknown domain"); return ARMON_ERR_PARAMS; }
+    if (which < 2 || which > 8) { set_error("a batch holds rho, umat, vmat, Emat, pmat, cmat, gmat only"); return ARMON_ERR_PARAMS; }
+    CUDA_TRY(cudaMemcpyAsync(&b->h_states[id], b->d_states + id, sizeof(StepState), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    Dom& d = b->doms[id];
+    int k = which <= 5 ? current_set(b, id) * 4 + (which - 2) : 8 + (which - 6);
+    size_t n = (size_t)d.p.nb_cells;
+    if (!b->fp32) {
+        CUDA_TRY(cudaMemcpyAsync(host, d.arr[k], n * 8, cudaMemcpyDeviceToHost, b->stream));
+        CUDA_TRY(cudaStreamSynchronize(b->stream));
+        return ARMON_OK;
+    }
+    std::vector<float> tmp(n);
+    CUDA_TRY(cudaMemcpyAsync(tmp.data(), d.arr[k], n * 4, cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    for (size_t i = 0; i < n; i++) host[i] = tmp[i];
+    return ARMON_OK;
+}
+
+int armon_batch_remove(armon_batch* b, int32_t id)
+{
+    if (id < 0 || id >= (int)b->doms.size() || !b->doms[id].used) { set_error("unknown domain"); return ARMON_ERR_PARAMS; }
+    Dom& d = b->doms[id];
+    CUDA_TRY(cudaFreeAsync(d.chunk, b->stream));
+    b->bytes -= d.bytes;
+    d = Dom();
+    b->dirty = true;
+    return ARMON_OK;
+}
+
+int32_t armon_batch_size(armon_batch* b)
+{
+    int n = 0;
+    for (auto& d : b->doms) n += d.used;
+    return n;
+}
+
+int64_t armon_batch_bytes_in_use(armon_batch* b) { return b->bytes; }
+int64_t armon_batch_kernel_launches(armon_batch* b) { return b->launches; }
+
+}  // extern "C"

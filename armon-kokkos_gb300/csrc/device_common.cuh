@@ -109,6 +109,17 @@ struct DtAcc {
         }
     }
     __device__ __forceinline__ void merge(double ox, double oy) { ax = kmax(ax, ox); ay = kmax(ay, oy); }
+    // The same for FP32 fields: the per-cell speeds in FP32 (FP64 arithmetic per cell would put
+    // the FP32 variant on GB300's 1/64-rate FP64 pipe), the maxima, dt and the step logic in FP64.
+    __device__ __forceinline__ void add(float u, float v, float c)
+    {
+        float mx = kmax(fabsf(u + c), fabsf(u - c));
+        float my = kmax(fabsf(v + c), fabsf(v - c));
+        if (mx == mx) {
+            ax = kmax(ax, double(mx));
+            if (my == my) ay = kmax(ay, double(my));
+        }
+    }
 };
 
 __host__ __device__ inline double dt_from_maxima(double ax, double ay, double dx, double dy)

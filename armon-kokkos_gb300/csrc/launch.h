@@ -16,6 +16,12 @@ cudaError_t launch_sweep(const SweepArgs<double>& a, int scheme, int proj, bool 
 cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
                          cudaStream_t st);
 
+// Fused axis pass over many domains (sweep_batch_kernel): doms / offsets are device arrays.
+cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
+                               int scheme, int proj, bool last, int block, cudaStream_t st);
+cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks, int pass,
+                               int scheme, int proj, bool last, int block, cudaStream_t st);
+
 // init_test over all nb_cells cells (src/kernels/init_test.cpp:51-104).
 struct InitPtrs {
     void *x, *y, *rho, *Emat, *umat, *vmat, *mask, *pmat, *cmat, *gmat, *ustar, *pstar;

@@ -16,6 +16,7 @@
 #include "armon_gb300.h"
 #include "host_common.h"
 #include "launch.h"
+#include "solver_common.h"
 
 using namespace armon;
 
@@ -59,106 +60,14 @@ int cuda_fail(cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail(e_, #expr);       \
     } while (0)
 
-// Cells the fused pass reads beyond the real ones along its axis: the reference's flux domain
-// (src/ranges.cpp:14-30) reaches one cell further than min_ghosts except for GAD + second order.
-int stencil_reach(const armon_params* p)
-{
-    return 2 + (p->scheme == ARMON_GAD) + (p->projection == ARMON_EULER_2ND);
-}
-
-bool is_pow2(double x)
-{
-    int e;
-    double m = std::frexp(x, &e);
-    return x > 0 && m == 0.5;
-}
-
-// Segments along the axis: minimise (most blocks on one SM) x (cells a thread walks, halo
-// included) over the segment count, with segments of at least 16 cells.
-void choose_segments(int n, int nlines, int block, int halo, int sms, int forced, int* seg_len, int* nseg, int* nlb)
-{
-    *nlb = std::max(1, (nlines + block - 1) / block);
-    if (forced > 0) {
-        *seg_len = std::min(forced, n);
-        *nseg = (n + *seg_len - 1) / *seg_len;
-        return;
-    }
-    double best = 1e300;
-    int best_seg = n;
-    for (int ns = 1; ns <= std::max(1, n / 16); ns++) {
-        int sl = (n + ns - 1) / ns;
-        if ((int64_t)sl * (ns - 1) >= n) continue;
-        int64_t blocks = (int64_t)(*nlb) * ns;
-        double per_sm = std::ceil(double(blocks) / sms);
-        double cost = per_sm * (sl + 1.2 * halo);
-        if (cost < best - 1e-9) { best = cost; best_seg = sl; }
-    }
-    *seg_len = best_seg;
-    *nseg = (n + best_seg - 1) / best_seg;
-}
-
 template <class T>
 void fill_geom(armon_solver* s, SweepArgs<T>& a)
 {
-    const armon_params& p = s->p;
-    const int halo = stencil_reach(&p);
-    for (int axis = 0; axis < 2; axis++) {
-        AxisGeom<T>& g = a.geom[axis];
-        g.n = axis == 0 ? p.nx : p.ny;
-        g.nlines = axis == 0 ? p.ny : p.nx;
-        g.s = axis == 0 ? 1 : p.row_length;
-        g.lstride = axis == 0 ? p.row_length : 1;
-        choose_segments(g.n, g.nlines, s->block, halo, s->sm_count, s->o.seg_len, &g.seg_len, &g.nseg, &g.nlb);
-        g.blocks = g.nlb * g.nseg;
-        // BC sign factors: X pass low = Left, high = Right; Y pass low = Bottom (y = -1), high = Top.
-        double lo_u, lo_v, hi_u, hi_v;
-        armon_boundary_factors(p.test, axis == 0 ? ARMON_LEFT : ARMON_BOTTOM, &lo_u, &lo_v);
-        armon_boundary_factors(p.test, axis == 0 ? ARMON_RIGHT : ARMON_TOP, &hi_u, &hi_v);
-        // axis velocity: umat in X, vmat in Y
-        g.fa_lo = T(axis == 0 ? lo_u : lo_v);
-        g.fo_lo = T(axis == 0 ? lo_v : lo_u);
-        g.fa_hi = T(axis == 0 ? hi_u : hi_v);
-        g.fo_hi = T(axis == 0 ? hi_v : hi_u);
-        double dx = (axis == 0 ? p.domain_size[0] / double(p.nx) : p.domain_size[1] / double(p.ny));
-        g.dx = T(dx);
-        g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;
-        g.inv_dx = g.dx_pow2 ? T(1.0 / double(g.dx)) : T(0);
-    }
-    a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
-    a.sw = p.stencil_width;
-    a.limiter = p.limiter;
-    a.npass = s->npass;
-    a.write_eos = 1;
-    a.gamma = T(1.4);   // update_EOS hard-codes gamma = 1.4 (src/armon_2D.cpp:94)
     T* const* arr = reinterpret_cast<T* const*>(s->arr);
     // set 0: rho umat vmat Emat; set 1: the four work arrays (free in the fused path)
-    a.buf[0][0] = arr[2]; a.buf[0][1] = arr[3]; a.buf[0][2] = arr[4]; a.buf[0][3] = arr[5];
-    a.buf[1][0] = arr[11]; a.buf[1][1] = arr[12]; a.buf[1][2] = arr[13]; a.buf[1][3] = arr[14];
-    a.pmat = arr[6]; a.cmat = arr[7]; a.gmat = arr[8];
-    a.state = s->d_state;
-    a.cfg = s->cfg;
-    a.partials = s->d_partials;
-    s->grid = std::max(a.geom[0].blocks, a.geom[1].blocks);
-}
-
-int check_supported(const armon_params* p)
-{
-    if (!armon_params_check(p)) { set_error("invalid parameters (Params::check)"); return ARMON_ERR_PARAMS; }
-    if (p->test == ARMON_BIZARRIUM) {
-        set_error("the fused solver implements the perfect-gas EOS only (Bizarrium is served by the stage kernels)");
-        return ARMON_ERR_UNSUPPORTED;
-    }
-    if (p->projection == ARMON_PROJ_NONE) { set_error("projection None is not supported"); return ARMON_ERR_UNSUPPORTED; }
-    const int halo = stencil_reach(p);
-    if (p->nb_ghosts < halo) {
-        set_error("the fused solver needs nb_ghosts >= " + std::to_string(halo) + " for this scheme");
-        return ARMON_ERR_UNSUPPORTED;
-    }
-    if (p->nx < p->stencil_width || p->ny < p->stencil_width) {
-        set_error("the fused solver needs nx, ny >= stencil_width (mirrored bands may not overlap)");
-        return ARMON_ERR_UNSUPPORTED;
-    }
-    return ARMON_OK;
+    DomainBuffers<T> b{{{arr[2], arr[3], arr[4], arr[5]}, {arr[11], arr[12], arr[13], arr[14]}}, arr[6], arr[7], arr[8]};
+    s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, s->o.seg_len, b, s->d_state, s->d_partials,
+                                 s->o.materialize_eos, a);
 }
 
 int sync_state(armon_solver* s)
@@ -296,15 +205,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     e = cudaMalloc(&s->d_state, sizeof(StepState));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_state, sizeof(StepState));
     // the partial buffers are sized after the geometry is known
-    s->cfg.cfl = p->cfl;
-    s->cfg.Dt = p->Dt;
-    s->cfg.max_time = p->max_time;
-    s->cfg.dt_dx = p->domain_size[0] / double(p->nx);
-    s->cfg.dt_dy = p->domain_size[1] / double(p->ny);
-    s->cfg.cst_dt = p->cst_dt;
-    s->cfg.dt_on_even_cycles = p->dt_on_even_cycles;
-    s->cfg.max_cycles = p->max_cycles;
-    s->cfg.splitting = p->axis_splitting;
+    s->cfg = make_step_config(*p);
     if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
     int pblocks = std::max(s->grid, s->sm_count * 8);
     s->cons_grid = s->sm_count * 4;
@@ -313,8 +214,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
     std::memset(s->h_state, 0, sizeof(StepState));
-    if (s->fp32) { s->a32.state = s->d_state; s->a32.partials = s->d_partials; s->a32.write_eos = s->o.materialize_eos; }
-    else { s->a64.state = s->d_state; s->a64.partials = s->d_partials; s->a64.write_eos = s->o.materialize_eos; }
+    if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
     *out = s;
     return ARMON_OK;
 }

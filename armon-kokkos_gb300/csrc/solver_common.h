@@ -1,0 +1,142 @@
+// solver_common.h -- host-side set-up shared by the single-domain solver (solver.cu) and the
+// batch (batch.cu): support checks, launch geometry and the fused pass's argument block.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "armon_gb300.h"
+#include "host_common.h"
+#include "sweep.cuh"
+
+namespace armon {
+
+// Cells the fused pass reads beyond the real ones along its axis: the reference's flux domain
+// (src/ranges.cpp:14-30) reaches one cell further than min_ghosts except for GAD + second order.
+inline int stencil_reach(const armon_params* p)
+{
+    return 2 + (p->scheme == ARMON_GAD) + (p->projection == ARMON_EULER_2ND);
+}
+
+inline bool is_pow2(double x)
+{
+    int e;
+    double m = std::frexp(x, &e);
+    return x > 0 && m == 0.5;
+}
+
+// Segments along the axis: minimise (most blocks on one SM) x (cells a thread walks, halo
+// included) over the segment count, with segments of at least 16 cells.
+inline void choose_segments(int n, int nlines, int block, int halo, int sms, int forced, int* seg_len, int* nseg,
+                            int* nlb)
+{
+    *nlb = std::max(1, (nlines + block - 1) / block);
+    if (forced > 0) {
+        *seg_len = std::min(forced, n);
+        *nseg = (n + *seg_len - 1) / *seg_len;
+        return;
+    }
+    double best = 1e300;
+    int best_seg = n;
+    for (int ns = 1; ns <= std::max(1, n / 16); ns++) {
+        int sl = (n + ns - 1) / ns;
+        if ((int64_t)sl * (ns - 1) >= n) continue;
+        int64_t blocks = (int64_t)(*nlb) * ns;
+        double per_sm = std::ceil(double(blocks) / sms);
+        double cost = per_sm * (sl + 1.2 * halo);
+        if (cost < best - 1e-9) { best = cost; best_seg = sl; }
+    }
+    *seg_len = best_seg;
+    *nseg = (n + best_seg - 1) / best_seg;
+}
+
+inline int check_supported(const armon_params* p)
+{
+    if (!armon_params_check(p)) { set_error("invalid parameters (Params::check)"); return ARMON_ERR_PARAMS; }
+    if (p->test == ARMON_BIZARRIUM) {
+        set_error("the fused solver implements the perfect-gas EOS only (Bizarrium is served by the stage kernels)");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    if (p->projection == ARMON_PROJ_NONE) { set_error("projection None is not supported"); return ARMON_ERR_UNSUPPORTED; }
+    const int halo = stencil_reach(p);
+    if (p->nb_ghosts < halo) {
+        set_error("the fused solver needs nb_ghosts >= " + std::to_string(halo) + " for this scheme");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    if (p->nx < p->stencil_width || p->ny < p->stencil_width) {
+        set_error("the fused solver needs nx, ny >= stencil_width (mirrored bands may not overlap)");
+        return ARMON_ERR_UNSUPPORTED;
+    }
+    return ARMON_OK;
+}
+
+inline StepConfig make_step_config(const armon_params& p)
+{
+    StepConfig c{};
+    c.cfl = p.cfl;
+    c.Dt = p.Dt;
+    c.max_time = p.max_time;
+    c.dt_dx = p.domain_size[0] / double(p.nx);
+    c.dt_dy = p.domain_size[1] / double(p.ny);
+    c.cst_dt = p.cst_dt;
+    c.dt_on_even_cycles = p.dt_on_even_cycles;
+    c.max_cycles = p.max_cycles;
+    c.splitting = p.axis_splitting;
+    return c;
+}
+
+// The state buffers of one domain: set 0 and set 1 of (rho, umat, vmat, Emat), and p, c, g.
+template <class T>
+struct DomainBuffers {
+    T* set[2][4];
+    T *pmat, *cmat, *gmat;
+};
+
+// Fills the argument block of the fused pass for one domain; returns the blocks it needs (the
+// larger of its two axes).
+template <class T>
+int make_sweep_args(const armon_params& p, int npass, int block, int sms, int forced_seg, const DomainBuffers<T>& b,
+                    StepState* state, double* partials, int write_eos, SweepArgs<T>& a)
+{
+    const int halo = stencil_reach(&p);
+    for (int axis = 0; axis < 2; axis++) {
+        AxisGeom<T>& g = a.geom[axis];
+        g.n = axis == 0 ? p.nx : p.ny;
+        g.nlines = axis == 0 ? p.ny : p.nx;
+        g.s = axis == 0 ? 1 : p.row_length;
+        g.lstride = axis == 0 ? p.row_length : 1;
+        choose_segments(g.n, g.nlines, block, halo, sms, forced_seg, &g.seg_len, &g.nseg, &g.nlb);
+        g.blocks = g.nlb * g.nseg;
+        // BC sign factors: X pass low = Left, high = Right; Y pass low = Bottom (y = -1), high = Top.
+        double lo_u, lo_v, hi_u, hi_v;
+        armon_boundary_factors(p.test, axis == 0 ? ARMON_LEFT : ARMON_BOTTOM, &lo_u, &lo_v);
+        armon_boundary_factors(p.test, axis == 0 ? ARMON_RIGHT : ARMON_TOP, &hi_u, &hi_v);
+        // axis velocity: umat in X, vmat in Y
+        g.fa_lo = T(axis == 0 ? lo_u : lo_v);
+        g.fo_lo = T(axis == 0 ? lo_v : lo_u);
+        g.fa_hi = T(axis == 0 ? hi_u : hi_v);
+        g.fo_hi = T(axis == 0 ? hi_v : hi_u);
+        double dx = (axis == 0 ? p.domain_size[0] / double(p.nx) : p.domain_size[1] / double(p.ny));
+        g.dx = T(dx);
+        g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;
+        g.inv_dx = g.dx_pow2 ? T(1.0 / double(g.dx)) : T(0);
+    }
+    a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
+    a.sw = p.stencil_width;
+    a.limiter = p.limiter;
+    a.npass = npass;
+    a.pass = 0;
+    a.write_eos = write_eos;
+    a.gamma = T(1.4);   // update_EOS hard-codes gamma = 1.4 (src/armon_2D.cpp:94)
+    for (int k = 0; k < 4; k++) { a.buf[0][k] = b.set[0][k]; a.buf[1][k] = b.set[1][k]; }
+    a.pmat = b.pmat;
+    a.cmat = b.cmat;
+    a.gmat = b.gmat;
+    a.state = state;
+    a.cfg = make_step_config(p);
+    a.partials = partials;
+    return std::max(a.geom[0].blocks, a.geom[1].blocks);
+}
+
+}  // namespace armon

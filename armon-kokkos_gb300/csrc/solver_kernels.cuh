@@ -74,7 +74,7 @@ __global__ void begin_kernel(BeginArgs a)
         pmat[idx] = p;
         cmat[idx] = c;
         gmat[idx] = (1 + gamma) / 2;
-        acc.add(double(umat[idx]), double(vmat[idx]), double(c));
+        acc.add(umat[idx], vmat[idx], c);
     }
     double gx, gy;
     if (grid_dt_maxima(acc, a.partials, &a.state->counter, &gx, &gy)) {
@@ -152,6 +152,30 @@ static cudaError_t launch_sweep_t(const SweepArgs<T>& a, int scheme, int proj, b
     }
     if (proj == 2) return last ? launch_one<T, 0, 2, true>(a, grid, block, st) : launch_one<T, 0, 2, false>(a, grid, block, st);
     return last ? launch_one<T, 0, 1, true>(a, grid, block, st) : launch_one<T, 0, 1, false>(a, grid, block, st);
+}
+
+template <class T, int S, int P, bool L>
+static cudaError_t launch_batch_one(const SweepArgs<T>* doms, const int* offsets, int ndom, int grid, int pass,
+                                    int block, cudaStream_t st)
+{
+    sweep_batch_kernel<T, S, P, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass);
+    return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t launch_sweep_batch_t(const SweepArgs<T>* doms, const int* offsets, int ndom, int grid, int pass,
+                                        int scheme, int proj, bool last, int block, cudaStream_t st)
+{
+#define ARMON_B(S, P)                                                                                  \
+    return last ? launch_batch_one<T, S, P, true>(doms, offsets, ndom, grid, pass, block, st)          \
+                : launch_batch_one<T, S, P, false>(doms, offsets, ndom, grid, pass, block, st)
+    if (scheme == 1) {
+        if (proj == 2) ARMON_B(1, 2);
+        ARMON_B(1, 1);
+    }
+    if (proj == 2) ARMON_B(0, 2);
+    ARMON_B(0, 1);
+#undef ARMON_B
 }
 
 }  // namespace armon

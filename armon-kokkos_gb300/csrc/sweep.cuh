@@ -224,9 +224,10 @@ __device__ __forceinline__ Adv<T> advect1(const Flux<T>& Fk, const Lag<T>& Lm, c
     return a;
 }
 
+// One axis pass of one domain, as block `blk` of the `nblk` blocks given to that domain.
 // Scheme 0 Godunov / 1 GAD; Proj 1 first order / 2 second order; LAST: the pass that ends a cycle.
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
+__device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int blk, const int nblk, const int pass)
 {
     constexpr bool kGAD = SCHEME == 1;
     constexpr bool kE2 = PROJ == 2;
@@ -242,17 +243,17 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
     const CycleDt cd = cycle_time_step(st, A.cfg);
     if (!cd.run) return;
     if (cd.invalid) {
-        if (LAST && blockIdx.x == 0 && threadIdx.x == 0) A.state->status = STATUS_INVALID_DT;
+        if (LAST && blk == 0 && threadIdx.x == 0) A.state->status = STATUS_INVALID_DT;
         return;
     }
 
     int axis;
     double factor;
-    split_axis(A.cfg.splitting, st.cycle, A.pass, &axis, &factor);
+    split_axis(A.cfg.splitting, st.cycle, pass, &axis, &factor);
     const AxisGeom<T>& g = A.geom[axis];
     const T dt = T(cd.current * factor);
     const T dx = g.dx;
-    const int src = (int)(((int64_t)st.cycle * A.npass + A.pass + st.buf_base) & 1);
+    const int src = (int)(((int64_t)st.cycle * A.npass + pass + st.buf_base) & 1);
     T* const* in = A.buf[src];
     T* const* out = A.buf[src ^ 1];
     // X pass: the axis velocity is umat (1), Y pass: vmat (2)
@@ -264,10 +265,10 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
     DtAcc acc;
     acc.init();
 
-    const int lb = blockIdx.x % max(g.nlb, 1);
-    const int seg = blockIdx.x / max(g.nlb, 1);
+    const int lb = blk % max(g.nlb, 1);
+    const int seg = blk / max(g.nlb, 1);
     const int line = lb * blockDim.x + threadIdx.x;
-    const bool active = blockIdx.x < g.blocks && line < g.nlines;
+    const bool active = blk < g.blocks && line < g.nlines;
 
     if (active) {
         const int n = g.n, sw = A.sw;
@@ -360,8 +361,8 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
                 out[3][idx] = E;
                 if (LAST) {
                     // dt_CFL of the state after this pass, with c from this pass's EOS
-                    if (axis == 0) acc.add(double(ua), double(uo), double(Lc.c));
-                    else acc.add(double(uo), double(ua), double(Lc.c));
+                    if (axis == 0) acc.add(ua, uo, Lc.c);
+                    else acc.add(uo, ua, Lc.c);
                 }
             }
         }
@@ -379,18 +380,18 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
     if (threadIdx.x == 0) {
         double ax = red[0][0], ay = red[1][0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) { ax = kmax(ax, red[0][w]); ay = kmax(ay, red[1][w]); }
-        A.partials[2 * blockIdx.x] = ax;
-        A.partials[2 * blockIdx.x + 1] = ay;
+        A.partials[2 * blk] = ax;
+        A.partials[2 * blk + 1] = ay;
         __threadfence();
         unsigned prev = atomicAdd(&A.state->counter, 1u);
-        is_last_block = (prev == gridDim.x - 1);
+        is_last_block = (prev == (unsigned)nblk - 1);
     }
     __syncthreads();
     if (!is_last_block) return;
     __threadfence();
     DtAcc tot;
     tot.init();
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
         tot.merge(__ldcg(&A.partials[2 * b]), __ldcg(&A.partials[2 * b + 1]));
     for (int o = 16; o > 0; o >>= 1)
         tot.merge(__shfl_xor_sync(0xffffffffu, tot.ax, o), __shfl_xor_sync(0xffffffffu, tot.ay, o));
@@ -409,6 +410,36 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
         ns.counter = 0;
         *A.state = ns;
     }
+}
+
+// One domain: the whole grid works on it.
+template <class T, int SCHEME, int PROJ, bool LAST>
+__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
+{
+    sweep_domain<T, SCHEME, PROJ, LAST>(A, blockIdx.x, gridDim.x, A.pass);
+}
+
+// Many independent domains in one launch.  Domain d owns blocks [offsets[d], offsets[d+1]) of the
+// grid (enough for its larger axis); each domain keeps its own step state, so dt, time and cycle
+// advance per domain and a finished domain's blocks return at once.
+template <class T, int SCHEME, int PROJ, bool LAST>
+__global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
+                                                          const int* __restrict__ offsets, int ndom, int pass)
+{
+    const int b = blockIdx.x;
+    int lo = 0, hi = ndom;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (offsets[mid] <= b) lo = mid; else hi = mid;
+    }
+    // the block's domain arguments in shared memory: read once, and not aliased by the stores
+    __shared__ __align__(16) SweepArgs<T> sA;
+    static_assert(sizeof(SweepArgs<T>) % 4 == 0, "word copy");
+    const int* src = reinterpret_cast<const int*>(&doms[lo]);
+    int* dst = reinterpret_cast<int*>(&sA);
+    for (int w = threadIdx.x; w < (int)(sizeof(SweepArgs<T>) / 4); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    sweep_domain<T, SCHEME, PROJ, LAST>(sA, b - offsets[lo], offsets[lo + 1] - offsets[lo], pass);
 }
 
 }  // namespace armon

@@ -11,6 +11,12 @@ cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool l
     return launch_sweep_t<float>(a, scheme, proj, last, grid, block, st);
 }
 
+cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks, int pass,
+                               int scheme, int proj, bool last, int block, cudaStream_t st)
+{
+    return launch_sweep_batch_t<float>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
+}
+
 cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st)
 {
     int64_t blocks = (ncells + 255) / 256;

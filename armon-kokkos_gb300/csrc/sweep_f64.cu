@@ -11,6 +11,12 @@ cudaError_t launch_sweep(const SweepArgs<double>& a, int scheme, int proj, bool 
     return launch_sweep_t<double>(a, scheme, proj, last, grid, block, st);
 }
 
+cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
+                               int scheme, int proj, bool last, int block, cudaStream_t st)
+{
+    return launch_sweep_batch_t<double>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
+}
+
 cudaError_t launch_init_f64(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st)
 {
     int64_t blocks = (ncells + 255) / 256;

@@ -139,6 +139,61 @@ int armon_solver_conservation(armon_solver* s, double* mass, double* energy);
 /* Number of kernels the solver launched so far (diagnostics). */
 int64_t armon_solver_kernel_launches(armon_solver* s);
 
+/* ---- batches: many independent domains advanced together (no counterpart in the reference;
+ *      each domain follows time_loop, src/armon_2D.cpp:327-386, on its own) ---- */
+typedef struct armon_batch armon_batch;
+
+typedef struct armon_batch_opts {
+    int32_t precision;        /* 64 or 32: every domain of a batch has this precision */
+    int32_t cycles_per_graph; /* cycles captured per CUDA graph launch (default 8) */
+    int32_t block_lines;      /* lines (threads) per block: a multiple of 32, at most 128 (default 128) */
+    int32_t seg_len;          /* cells per thread along the sweep axis for every domain (0 = per domain) */
+    int64_t memory_budget;    /* bytes of domain state the batch may hold (0 = no limit) */
+} armon_batch_opts;
+
+void armon_batch_opts_default(armon_batch_opts* o);
+int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch** out);
+void armon_batch_destroy(armon_batch* b);
+
+/* Device bytes a domain with these parameters holds in a batch of the given precision. */
+int64_t armon_batch_domain_bytes(const armon_params* p, int32_t precision);
+
+/* Adds a domain and starts its time loop: allocates its state from the stream-ordered pool
+ * (ARMON_ERR_NOMEM when the batch's budget would be exceeded), initialises it with init_test or,
+ * when `init` is not NULL, with the host FP64 arrays rho, umat, vmat, Emat (nb_cells values each,
+ * the reference's layout), then runs the EOS and the first dt.  All domains of a batch share
+ * scheme, projection and axis splitting.  *id receives the domain's handle. */
+int armon_batch_add(armon_batch* b, const armon_params* p, const double* const init[4], int32_t* id);
+
+/* Cells per thread along the sweep axis for one domain (0 = automatic); takes effect at the next
+ * launch.  Results do not depend on it. */
+int armon_batch_set_seg_len(armon_batch* b, int32_t id, int32_t seg_len);
+
+/* Enqueues n cycles of every domain whose loop is still running (no host synchronisation). */
+int armon_batch_enqueue_cycles(armon_batch* b, int32_t n);
+
+/* Runs until no domain's loop condition holds (or cycle_limit cycles were issued, if > 0), reading
+ * the domain states back once per graph batch.  *running receives the domains still running. */
+int armon_batch_run(armon_batch* b, int32_t cycle_limit, int32_t* running);
+
+/* Reads back all domain states; *running receives how many loops are still running. */
+int armon_batch_poll(armon_batch* b, int32_t* running);
+
+/* State of one domain as of the last poll / run (cycle, time, dts in p; status 0 running or done,
+ * 1 invalid dt). */
+int armon_batch_domain_state(armon_batch* b, int32_t id, armon_params* p, int32_t* status);
+int armon_batch_domain_done(armon_batch* b, int32_t id);
+
+/* Downloads one array of a domain (which: 2 rho, 3 umat, 4 vmat, 5 Emat, 6 pmat, 7 cmat, 8 gmat). */
+int armon_batch_download(armon_batch* b, int32_t id, int which, double* host);
+
+/* Frees a domain's state (stream-ordered) and its handle. */
+int armon_batch_remove(armon_batch* b, int32_t id);
+
+int32_t armon_batch_size(armon_batch* b);                /* domains held */
+int64_t armon_batch_bytes_in_use(armon_batch* b);
+int64_t armon_batch_kernel_launches(armon_batch* b);
+
 /* One full solve with host buffers, the reference-facing end-to-end call: uploads rho, umat,
  * vmat, Emat (and the rest of the initial state made by init_test on the device), runs the time
  * loop and downloads rho, umat, vmat, Emat, pmat.  Arrays have nb_cells values in the

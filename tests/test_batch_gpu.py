@@ -1,0 +1,121 @@
+"""The batched multi-domain step (armon_batch_*): every domain of a batch must give what it gives
+alone, bit for bit in FP64, and what the oracle gives for the same initial state."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import armon_gb300 as A
+import oracle_lib as O
+from armon_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("rho", "umat", "vmat", "Emat", "pmat")
+
+
+def small_domains(n, seed, sides=(16, 24, 40, 64, 96), t_end=0.15):
+    ds = W.mixed_domains(n, seed=seed, sides=sides)
+    for k, d in enumerate(ds):
+        d.t_end = t_end * (0.5 + 0.5 * (k % 3) / 2)   # different end times: domains finish apart
+    return ds
+
+
+def solo(spec, precision=64, seg_len=0):
+    with A.Solver(spec.params(), precision=precision, seg_len=seg_len) as s:
+        s.init_test()
+        for k, a in spec.initial_state().items():
+            s.upload(k, a)
+        s.begin_loop()
+        s.run()
+        p, st = s.state()
+        return p, st, {k: A.real_cells(s.params, s.download(k)) for k in FIELDS}
+
+
+def oracle(spec):
+    L = O.lib()
+    p = O.make_params(O.Case(**spec.case().__dict__))
+    st = O.OracleState(p)
+    L.o_init_test_p(C.byref(p), C.byref(st.data), 0)
+    for k, a in spec.initial_state().items():
+        st[k][:] = a
+    status = C.c_int()
+    L.o_time_loop(C.byref(p), C.byref(st.data), C.byref(status))
+    assert status.value == 0
+    return p, {k: O.real_cells(p, st[k]) for k in FIELDS}
+
+
+def test_batch_domains_match_solo_runs_bitwise():
+    specs = small_domains(14, seed=11)
+    with A.Batch(cycles_per_graph=4) as b:
+        ids = [b.add(s.params(), s.initial_state()) for s in specs]
+        assert b.run() == 0
+        for i, spec in zip(ids, specs):
+            pb, stb = b.state(i)
+            ps, sts, ref = solo(spec)
+            assert stb == 0 and sts == 0
+            assert pb.cycle == ps.cycle and pb.time == ps.time and pb.next_cycle_dt == ps.next_cycle_dt
+            for k in FIELDS:
+                got = A.real_cells(b.params[i], b.download(i, k))
+                assert np.array_equal(got.view(np.int64), ref[k].view(np.int64)), (spec, k)
+        assert b.kernel_launches > 0
+
+
+def test_batch_domain_matches_oracle():
+    spec = small_domains(3, seed=5, sides=(48, 80))[2]
+    po, ref = oracle(spec)
+    with A.Batch() as b:
+        i = b.add(spec.params(), spec.initial_state())
+        b.run()
+        pb, st = b.state(i)
+        assert st == 0 and pb.cycle == po.cycle and pb.next_cycle_dt == po.next_cycle_dt
+        for k in FIELDS:
+            assert np.array_equal(A.real_cells(b.params[i], b.download(i, k)), ref[k]), k
+
+
+def test_batch_admission_removal_and_budget():
+    specs = small_domains(6, seed=3)
+    per = [A.domain_bytes(s.params()) for s in specs]
+    budget = sum(per[:3]) + per[3] // 2
+    with A.Batch(memory_budget=budget) as b:
+        ids = [b.add(s.params(), s.initial_state()) for s in specs[:3]]
+        with pytest.raises(A.ArmonError) as ei:
+            b.add(specs[3].params(), specs[3].initial_state())
+        assert ei.value.code == A.ERR_NOMEM
+        b.run(cycle_limit=5)
+        b.remove(ids[1])                      # frees a slot and its memory
+        assert b.bytes_in_use == per[0] + per[2]
+        j = b.add(specs[4].params(), specs[4].initial_state())   # admitted while others are mid-run
+        assert j == ids[1]                    # slot reused
+        assert b.run() == 0
+        for i, spec in ((ids[0], specs[0]), (ids[2], specs[2]), (j, specs[4])):
+            ps, _, ref = solo(spec)
+            pb, _ = b.state(i)
+            assert pb.cycle == ps.cycle
+            for k in FIELDS:
+                assert np.array_equal(A.real_cells(b.params[i], b.download(i, k)), ref[k]), k
+
+
+def test_batch_fp32_close_to_solo_fp32():
+    specs = small_domains(5, seed=21)
+    with A.Batch(precision=32) as b:
+        ids = [b.add(s.params(), s.initial_state()) for s in specs]
+        b.run()
+        for i, spec in zip(ids, specs):
+            ps, _, ref = solo(spec, precision=32)
+            pb, _ = b.state(i)
+            assert pb.cycle == ps.cycle
+            for k in ("rho", "Emat"):
+                got = A.real_cells(b.params[i], b.download(i, k))
+                assert np.allclose(got, ref[k], rtol=1e-6, atol=0), k
+
+
+def test_batch_segment_choice_does_not_change_results():
+    spec = small_domains(1, seed=9, sides=(96,))[0]
+    _, _, ref = solo(spec)
+    with A.Batch() as b:
+        i = b.add(spec.params(), spec.initial_state())
+        b.set_seg_len(i, 17)
+        b.run()
+        for k in FIELDS:
+            assert np.array_equal(A.real_cells(b.params[i], b.download(i, k)), ref[k]), k

@@ -32,6 +32,7 @@ UNITS = [
     ("abi_kernels.cu", ["--fmad=false"]),
     ("solver.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),
+    ("selftest.cu", ["--fmad=false"]),
     ("params.cpp", []),
     ("armon_2D.cpp", []),
 ]

@@ -101,11 +101,23 @@ struct DtAcc {
     __device__ __forceinline__ void init() { ax = 0.0; ay = 0.0; }
     __device__ __forceinline__ void add(double u, double v, double c)
     {
-        double mx = kmax(fabs(u + c), fabs(u - c));
-        double my = kmax(fabs(v + c), fabs(v - c));
-        if (mx == mx) {
-            ax = kmax(ax, mx);
-            if (my == my) ay = kmax(ay, my);
+        // kmax of non-negative values: for sign-clear, non-NaN doubles the IEEE order is the
+        // unsigned order of the bit patterns, so the compares run on the integer pipes
+        const uint64_t inf = 0x7FF0000000000000ull;
+        const uint64_t a1 = (uint64_t)__double_as_longlong(fabs(u + c));
+        const uint64_t a2 = (uint64_t)__double_as_longlong(fabs(u - c));
+        const uint64_t b1 = (uint64_t)__double_as_longlong(fabs(v + c));
+        const uint64_t b2 = (uint64_t)__double_as_longlong(fabs(v - c));
+        // kmax(a1, a2) = (a1 < a2) ? a2 : a1, where a NaN a1 is kept and a NaN a2 is not taken
+        const uint64_t mx = (a1 <= inf && a2 <= inf && a1 < a2) ? a2 : a1;
+        const uint64_t my = (b1 <= inf && b2 <= inf && b1 < b2) ? b2 : b1;
+        if (mx <= inf) {
+            const uint64_t cur = (uint64_t)__double_as_longlong(ax);
+            if (cur < mx) ax = __longlong_as_double((long long)mx);
+            if (my <= inf) {
+                const uint64_t cy = (uint64_t)__double_as_longlong(ay);
+                if (cy < my) ay = __longlong_as_double((long long)my);
+            }
         }
     }
     __device__ __forceinline__ void merge(double ox, double oy) { ax = kmax(ax, ox); ay = kmax(ay, oy); }

@@ -1,0 +1,135 @@
+// selftest.cu -- checks of the integer-pipe FP64 operations (softfp.cuh) against the FP64
+// instructions, on generated operands.  Exposed as armon_selftest_softfp for the test suite.
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "softfp.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix(uint64_t x)
+{
+    // splitmix64 finaliser
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double normal_double(uint64_t r, int exp_span)
+{
+    // random sign and significand, exponent uniform in [1023 - span, 1023 + span]
+    uint64_t e = 1023 - exp_span + (uint64_t)((r >> 53) % (uint64_t)(2 * exp_span + 1));
+    return armon::sfp::from_bits((r & 0x8000000000000000ull) | (e << 52) | (r & armon::sfp::kMant));
+}
+
+__device__ void operands(int mode, uint64_t seed, uint64_t i, double& a, double& b)
+{
+    using namespace armon::sfp;
+    uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1)), r3 = mix(r1 ^ r2);
+    switch (mode) {
+    case 0:   // random normal operands
+        a = normal_double(r1, 40);
+        b = normal_double(r2, 40);
+        break;
+    case 1:   // random bit patterns: zeros, subnormals, infinities, NaN
+        a = from_bits(r1);
+        b = from_bits(r2);
+        if ((r3 & 7) == 0) a = from_bits(r1 & 0x800FFFFFFFFFFFFFull);   // subnormal or zero
+        if ((r3 & 7) == 1) b = from_bits(r2 & 0x800FFFFFFFFFFFFFull);
+        if ((r3 & 15) == 2) a = from_bits((r1 & 0x8000000000000000ull) | 0x7FF0000000000000ull);
+        break;
+    case 2: {  // quotients near the midpoint between two doubles
+        b = normal_double(r2, 20);
+        double q = normal_double(r1, 20);
+        uint64_t uq = bits(q);
+        double half_ulp = from_bits((uq & 0x7FF0000000000000ull) - (53ull << 52));   // 2^(e_q - 53)
+        a = fma(b, q, b * half_ulp * ((r3 & 1) ? 1.0 : -1.0));
+        break;
+    }
+    case 3: {  // exact quotients: short significands
+        uint64_t qm = (r1 >> 38) | 1, bm = (r2 >> 38) | 1;    // 26-bit odd integers
+        double q = (double)qm * ((r3 & 1) ? 1.0 : -1.0), bb = (double)bm;
+        b = ldexp(bb, (int)(r3 >> 8) % 64 - 32);
+        a = q * b;
+        break;
+    }
+    case 4:   // power-of-two divisors
+        a = normal_double(r1, 60);
+        b = from_bits((r2 & 0x8000000000000000ull) | ((uint64_t)(1023 - 60 + (r2 >> 53) % 121) << 52));
+        break;
+    case 5:   // zero dividends and large exponent differences
+        a = (r3 & 1) ? normal_double(r1, 1000) : from_bits(r1 & 0x8000000000000000ull);
+        b = normal_double(r2, 1000);
+        break;
+    default:  // the operand ranges of the solver: O(1e-6 .. 1e3), both signs
+        a = normal_double(r1, 10) * 1e-3;
+        b = normal_double(r2, 10);
+        break;
+    }
+}
+
+__global__ void div_check(int mode, uint64_t seed, int64_t n, unsigned long long* out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a, b;
+        operands(mode, seed, (uint64_t)i, a, b);
+        double s = armon::sfp::div(a, b);
+        double h = a / b;
+        bool same = armon::sfp::bits(s) == armon::sfp::bits(h) || (s != s && h != h);
+        if (!same) {
+            if (atomicAdd(&out[0], 1ull) == 0) {
+                out[2] = armon::sfp::bits(a);
+                out[3] = armon::sfp::bits(b);
+            }
+        }
+        // operands the fast path takes (normal or zero dividend, normal divisor, quotient in range)
+        uint64_t ua = armon::sfp::bits(a), ub = armon::sfp::bits(b);
+        uint32_t ea = (uint32_t)(ua >> 52) & 0x7FF, eb = (uint32_t)(ub >> 52) & 0x7FF;
+        int e0 = (int)ea - (int)eb;
+        bool fast = (eb - 1u) < 2046u && ((ua << 1) == 0 || ((ea - 1u) < 2046u && e0 >= -1021 && e0 <= 1022));
+        if (fast) atomicAdd(&out[1], 1ull);
+    }
+}
+
+__global__ void cmp_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1)), r3 = mix(r1 ^ r2);
+        double x = from_bits(r1), y = (r3 & 3) == 0 ? from_bits(r1 ^ (r3 & 0x8000000000000000ull)) : from_bits(r2);
+        if ((r3 & 12) == 4) y = from_bits(r1 + (r3 >> 60) - 8);     // neighbours
+        if ((r3 & 48) == 16) x = from_bits(r3 & 0x8000000000000000ull);   // +-0
+        // neg_if is the multiply by -1 for non-NaN x (a NaN's sign and payload are not portable)
+        bool ok = lt(x, y) == (x < y) && gt0(x) == (x > 0.0) &&
+                  (x != x || bits(neg_if(x, (r3 >> 7) & 1)) == bits((r3 >> 7) & 1 ? -x : x));
+        if (!ok && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = bits(x);
+            out[3] = bits(y);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// mode 0..6 (see operands) checks sfp::div against the hardware quotient; mode 100 checks lt,
+// gt0 and neg_if against the IEEE comparisons.  out[0] = mismatches, out[1] = fast-path operand
+// pairs, out[2..3] = the bits of the first mismatching operands.  Returns a cudaError_t.
+int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_host)
+{
+    unsigned long long* out = nullptr;
+    cudaError_t e = cudaMalloc(&out, 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return (int)e;
+    cudaMemset(out, 0, 4 * sizeof(unsigned long long));
+    if (mode == 100) cmp_check<<<152 * 16, 256>>>(seed, n, out);
+    else div_check<<<152 * 16, 256>>>(mode, seed, n, out);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out_host, out, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(out);
+    return (int)e;
+}
+
+}  // extern "C"

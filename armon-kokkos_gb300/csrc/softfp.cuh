@@ -1,0 +1,132 @@
+// softfp.cuh -- exact IEEE-754 binary64 operations on the integer and FP32 pipes.
+//
+// GB300 executes FP64 arithmetic at 1/64 of its FP32 rate (2 DFMA per SM per clock), and an IEEE
+// double division costs about 9 DFMA slots there, while the integer and FP32 pipes of the fused
+// pass are almost idle.  The helpers below compute bit-identical results to the FP64 instructions
+// they replace, for the operands the fast paths accept, using integer arithmetic:
+//
+//   lt(x, y)      x < y  (false when either is NaN; -0 == +0)
+//   gt0(x)        x > 0
+//   neg_if(x, c)  c ? -x : x  (a sign flip: what multiplying by -1 gives for non-NaN x)
+//   div(a, b)     the correctly rounded quotient (round to nearest, ties to even)
+//
+// Division (my own construction from the arithmetic, not a library's sequence).  With
+// significands ma, mb in [2^52, 2^53) and ma doubled when ma < mb, the result significand is
+// Q = floor(ma * 2^52 / mb) rounded with the remainder R = ma * 2^52 - Q * mb.  Q is estimated
+// with a reciprocal of d = mb * 2^11: an FP32 seed (rcp.approx of the top 24 bits), biased below
+// the true value, then two Newton steps y <- y + y (1 - d y) in 64-bit fixed point, each of which
+// keeps the estimate below 2^128 / d; then Q_est = floor(U * V / 2^128) for U = ma * 2^63.  The
+// remainder is computed exactly in 64 bits and Q_est is raised while R >= mb.  If R still is not
+// in [0, mb) -- which the error bounds exclude -- the hardware division is used, so a fast-path
+// result always satisfies ma * 2^52 = Q * mb + R with 0 <= R < mb, i.e. Q is exact.  Zero
+// dividends are handled; subnormal, infinite and NaN operands and quotients outside the normal
+// range go to the hardware division.
+#pragma once
+
+#include <cstdint>
+
+namespace armon {
+namespace sfp {
+
+__device__ __forceinline__ uint64_t bits(double x) { return (uint64_t)__double_as_longlong(x); }
+__device__ __forceinline__ double from_bits(uint64_t u) { return __longlong_as_double((long long)u); }
+
+constexpr uint64_t kAbs = 0x7FFFFFFFFFFFFFFFull;
+constexpr uint64_t kInf = 0x7FF0000000000000ull;
+constexpr uint64_t kMant = 0x000FFFFFFFFFFFFFull;
+constexpr uint64_t kHidden = 0x0010000000000000ull;
+
+// Monotone key of a non-NaN double: -x and +x map to -k and +k, and -0, +0 both to 0.
+__device__ __forceinline__ int64_t key(uint64_t u)
+{
+    const int64_t a = (int64_t)(u & kAbs);
+    return (int64_t)u < 0 ? -a : a;
+}
+
+__device__ __forceinline__ bool lt(double x, double y)
+{
+    const uint64_t ux = bits(x), uy = bits(y);
+    const bool nan = ((ux & kAbs) > kInf) | ((uy & kAbs) > kInf);
+    return !nan && key(ux) < key(uy);
+}
+
+__device__ __forceinline__ bool gt0(double x)
+{
+    const int64_t u = (int64_t)bits(x);
+    return u > 0 && (uint64_t)u <= kInf;
+}
+
+__device__ __forceinline__ double neg_if(double x, bool c)
+{
+    return from_bits(bits(x) ^ ((uint64_t)c << 63));
+}
+
+__device__ __forceinline__ double div(double a, double b)
+{
+    const uint64_t ua = bits(a), ub = bits(b);
+    const uint32_t ea = (uint32_t)(ua >> 52) & 0x7FFu;
+    const uint32_t eb = (uint32_t)(ub >> 52) & 0x7FFu;
+    const uint64_t sign = (ua ^ ub) & ~kAbs;
+    const int e0 = (int)ea - (int)eb;
+    const bool b_normal = (eb - 1u) < 2046u;
+    if (b_normal && (ua << 1) == 0) return from_bits(sign);   // +-0 / normal
+    if (!(b_normal && (ea - 1u) < 2046u && e0 >= -1021 && e0 <= 1022)) return a / b;
+
+    uint64_t ma = (ua & kMant) | kHidden;
+    const uint64_t mb = (ub & kMant) | kHidden;
+    int e = e0;
+    if (ma < mb) {
+        ma <<= 1;
+        e -= 1;
+    }
+    uint64_t q;
+    uint64_t r;
+    if (mb == kHidden) {
+        // a power-of-two divisor: the quotient is the dividend's significand, exactly
+        q = ma;
+        r = 0;
+    } else {
+        const uint64_t d = mb << 11;                                   // [2^63, 2^64)
+        const uint32_t top = (uint32_t)(d >> 40);                      // [2^23, 2^24)
+        const float fd = __uint_as_float(0x4B000000u | (top & 0x7FFFFFu));   // == top
+        float rf;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(fd));
+        const uint32_t urf = __float_as_uint(rf);
+        // V = 2^64 + v ~ 2^128 / d.  rf in (2^-24, 2^-23]; rf * 2^88 = 2^64 (1 + m 2^-23) when
+        // rf < 2^-23.  The seed is lowered by 2^44 (2^-21 relative) so that it is below 2^128 / d.
+        uint64_t v;
+        if ((urf >> 23) >= 104u) {
+            v = 0xFFFFF00000000000ull;
+        } else {
+            const uint64_t m = (uint64_t)(urf & 0x7FFFFFu) << 41;
+            v = m > (1ull << 44) ? m - (1ull << 44) : 0;
+        }
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            // e = 2^128 - d (2^64 + v) >= 0; its high word, then V += V e / 2^128 (from below)
+            const uint64_t ph = __umul64hi(d, v);
+            const uint64_t pl = d * v;
+            const uint64_t eh = 0ull - d - ph - (pl != 0 ? 1ull : 0ull);
+            v = v + eh + __umul64hi(v, eh);
+        }
+        // Q_est = floor((ma 2^63)(2^64 + v) / 2^128), dropping the low word of the dividend
+        const uint64_t u1 = ma >> 1;
+        q = u1 + __umul64hi(u1, v);
+        r = (ma << 52) - q * mb;          // exact: the true remainder lies in [0, 2^56)
+#pragma unroll
+        for (int it = 0; it < 3; it++) {
+            const bool up = r >= mb;
+            r = up ? r - mb : r;
+            q = up ? q + 1 : q;
+        }
+        if (r >= mb) return a / b;        // outside the error bounds: the hardware decides
+    }
+    // round to nearest, ties to even, on the exact remainder
+    const uint64_t r2 = r << 1;
+    const bool up = r2 > mb || (r2 == mb && (q & 1));
+    q += up ? 1ull : 0ull;
+    return from_bits(sign + ((uint64_t)(e + 1022) << 52) + q);
+}
+
+}  // namespace sfp
+}  // namespace armon

@@ -117,6 +117,13 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, int fo
         g.fo_lo = T(axis == 0 ? lo_v : lo_u);
         g.fa_hi = T(axis == 0 ? hi_u : hi_v);
         g.fo_hi = T(axis == 0 ? hi_v : hi_u);
+        const double f[4] = {double(g.fa_lo), double(g.fo_lo), double(g.fa_hi), double(g.fo_hi)};
+        g.fneg = 0;
+        g.f_unit = 1;
+        for (int k = 0; k < 4; k++) {
+            if (f[k] == -1.0) g.fneg |= 1u << k;
+            else if (f[k] != 1.0) g.f_unit = 0;
+        }
         double dx = (axis == 0 ? p.domain_size[0] / double(p.nx) : p.domain_size[1] / double(p.ny));
         g.dx = T(dx);
         g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;

@@ -35,6 +35,11 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "softfp.cuh"
+
+#ifndef ARMON_SOFT_FP64
+#define ARMON_SOFT_FP64 1
+#endif
 
 namespace armon {
 
@@ -51,6 +56,8 @@ struct AxisGeom {
     T fa_lo, fo_lo, fa_hi, fo_hi;   // sign factors of the axis / other velocity, low / high side
     T dx, inv_dx;       // p.dx of the axis; 1/dx when dx is a power of two
     int32_t dx_pow2;
+    uint32_t fneg;      // bit k set: factor k (fa_lo, fo_lo, fa_hi, fo_hi) is -1
+    int32_t f_unit;     // every factor is +1 or -1: apply them as sign flips
     int32_t pad;
 };
 
@@ -78,36 +85,47 @@ template <class T> struct Flux { T us, ps, psus, dtus; };    // psus = p* u*, dt
 template <class T> struct Lag { T rho, ua, uo, E, rua, ruo, rE, W, c; };
 template <class T> struct Adv { T r, ra, ro, rE; };
 
+// Operations that the FP64 pass routes to the integer pipes (softfp.cuh: GB300's FP64 pipe is the
+// bottleneck, its integer and FP32 pipes are idle) and the FP32 pass keeps on the FP32 pipe.  Both
+// give the IEEE results of the plain operators (for non-NaN operands where noted there).
+__device__ __forceinline__ double qdiv(double a, double b) { return ARMON_SOFT_FP64 ? sfp::div(a, b) : a / b; }
+__device__ __forceinline__ float qdiv(float a, float b) { return a / b; }
+__device__ __forceinline__ bool qlt(double a, double b) { return ARMON_SOFT_FP64 ? sfp::lt(a, b) : a < b; }
+__device__ __forceinline__ bool qlt(float a, float b) { return a < b; }
+__device__ __forceinline__ bool qgt0(double a) { return ARMON_SOFT_FP64 ? sfp::gt0(a) : a > 0.0; }
+__device__ __forceinline__ bool qgt0(float a) { return a > 0.0f; }
+__device__ __forceinline__ double qneg_if(double x, bool c) { return ARMON_SOFT_FP64 ? sfp::neg_if(x, c) : (c ? -x : x); }
+__device__ __forceinline__ float qneg_if(float x, bool c) { return c ? -x : x; }
+__device__ __forceinline__ bool qsignbit(double x) { return (int64_t)sfp::bits(x) < 0; }
+__device__ __forceinline__ bool qsignbit(float x) { return (int32_t)__float_as_uint(x) < 0; }
+// Kokkos::min / Kokkos::max: (b < a) ? b : a and (a < b) ? b : a
+template <class T> __device__ __forceinline__ T qmin(T a, T b) { return qlt(b, a) ? b : a; }
+template <class T> __device__ __forceinline__ T qmax(T a, T b) { return qlt(a, b) ? b : a; }
+
 template <class T>
 __device__ __forceinline__ T limiter_fn(int L, T r)
 {
     // src/kernels/limiters.h:15-34
-    if (L == 1) return kmax(T(0), kmin(T(1), r));
-    if (L == 2) return kmax(kmax(T(0), kmin(T(1), 2 * r)), kmin(T(2), r));
+    if (L == 1) return qmax(T(0), qmin(T(1), r));
+    if (L == 2) return qmax(qmax(T(0), qmin(T(1), 2 * r)), qmin(T(2), r));
     return T(1);
 }
 
 template <class T>
 __device__ __forceinline__ T slope_minmod(T u_im, T u_i, T u_ip, T r_m, T r_p)
 {
-    // src/kernels/euler_projection.cpp:73-79
+    // src/kernels/euler_projection.cpp:73-79.  s = copysign(1, D_u_p) is +-1, so s * v is v with
+    // its sign flipped when D_u_p's sign bit is set (bit-identical to the multiply for non-NaN v).
     T D_u_p = r_p * (u_ip - u_i);
     T D_u_m = r_m * (u_i - u_im);
-    T s = copysign(T(1), D_u_p);
-    return s * kmax(T(0), kmin(s * D_u_p, s * D_u_m));
-}
-
-template <class T>
-__device__ __forceinline__ T apply_factor(T v, T f)
-{
-    // u * factor for the sign factors +-1 without an FP multiply (exact for non-NaN v)
-    return f == T(1) ? v : (f == T(-1) ? -v : v * f);
+    const bool neg = qsignbit(D_u_p);
+    return qneg_if(qmax(T(0), qmin(qneg_if(D_u_p, neg), qneg_if(D_u_m, neg))), neg);
 }
 
 template <class T>
 __device__ __forceinline__ T div_dx(T x, const AxisGeom<T>& g)
 {
-    return g.dx_pow2 ? x * g.inv_dx : x / g.dx;
+    return g.dx_pow2 ? x * g.inv_dx : qdiv(x, g.dx);
 }
 
 template <class T>
@@ -116,7 +134,7 @@ __device__ __forceinline__ void eos(CellIn<T>& c, T gamma)
     // src/kernels/fluid_eos.cpp:18-21
     T e = c.E - T(0.5) * (c.ua * c.ua + c.uo * c.uo);
     c.p = (gamma - 1) * c.rho * e;
-    c.c = sqrt(gamma * c.p / c.rho);
+    c.c = sqrt(qdiv(gamma * c.p, c.rho));
 }
 
 template <class T>
@@ -127,8 +145,8 @@ __device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R
     T rc_l = L.rho * L.c;
     T rc_r = R.rho * R.c;
     g.rcs = rc_l + rc_r;
-    g.us = (rc_l * L.ua + rc_r * R.ua + (L.p - R.p)) / g.rcs;
-    g.ps = (rc_r * L.p + rc_l * R.p + rc_l * rc_r * (L.ua - R.ua)) / g.rcs;
+    g.us = qdiv(rc_l * L.ua + rc_r * R.ua + (L.p - R.p), g.rcs);
+    g.ps = qdiv(rc_r * L.p + rc_l * R.p + rc_l * rc_r * (L.ua - R.ua), g.rcs);
     return g;
 }
 
@@ -137,10 +155,10 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gm, const God<T>& Gc, const
                                        const CellIn<T>& Cl, const CellIn<T>& Cr, int L, T dt, T dx)
 {
     // src/kernels/acoustic.cpp:40-88 (face between Cl = i-s and Cr = i)
-    T r_um = (Gp.us - Cr.ua) / (Gc.us - Cl.ua + T(1e-6));
-    T r_pm = (Gp.ps - Cr.p) / (Gc.ps - Cl.p + T(1e-6));
-    T r_up = (Cl.ua - Gm.us) / (Cr.ua - Gc.us + T(1e-6));
-    T r_pp = (Cl.p - Gm.ps) / (Cr.p - Gc.ps + T(1e-6));
+    T r_um = qdiv(Gp.us - Cr.ua, Gc.us - Cl.ua + T(1e-6));
+    T r_pm = qdiv(Gp.ps - Cr.p, Gc.ps - Cl.p + T(1e-6));
+    T r_up = qdiv(Cl.ua - Gm.us, Cr.ua - Gc.us + T(1e-6));
+    T r_pp = qdiv(Cl.p - Gm.ps, Cr.p - Gc.ps + T(1e-6));
     r_um = limiter_fn(L, r_um);
     r_pm = limiter_fn(L, r_pm);
     r_up = limiter_fn(L, r_up);
@@ -148,7 +166,7 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gm, const God<T>& Gc, const
     T dm_l = Cl.rho * dx;
     T dm_r = Cr.rho * dx;
     T Dm = (dm_l + dm_r) * T(0.5);                       // (dm_l + dm_r) / 2
-    T theta = T(0.5) * (1 - (Gc.rcs * T(0.5)) * (dt / Dm));
+    T theta = T(0.5) * (1 - (Gc.rcs * T(0.5)) * qdiv(dt, Dm));
     Flux<T> f;
     f.us = Gc.us + theta * (r_up * (Cr.ua - Gc.us) - r_um * (Gc.us - Cl.ua));
     f.ps = Gc.ps + theta * (r_pp * (Cr.p - Gc.ps) - r_pm * (Gc.ps - Cl.p));
@@ -162,8 +180,8 @@ __device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0
     Lag<T> l;
     T dm = C.rho * dx;
     l.W = dx + dt * (F1.us - F0.us);
-    l.rho = dm / l.W;
-    T dtdm = dt / dm;
+    l.rho = qdiv(dm, l.W);
+    T dtdm = qdiv(dt, dm);
     l.ua = C.ua + dtdm * (F0.ps - F1.ps);
     l.E = C.E + dtdm * (F0.psus - F1.psus);
     l.uo = C.uo;
@@ -191,17 +209,17 @@ __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, 
 {
     // src/kernels/euler_projection.cpp:82-120 for face k; L0..L3 = cells k-2..k+1
     T disp = Fk.dtus;
-    bool up = disp > 0;
+    bool up = qgt0(disp);
     T Dx = up ? -(dx - Fm.dtus) : dx + Fp.dtus;
     Lag<T> Cm = sel(up, L0, L1), Ci = sel(up, L1, L2), Cp = sel(up, L2, L3);
     T Dx_lm = Cm.W, Dx_l = Ci.W, Dx_lp = Cp.W;
-    T r_m = (2 * Dx_l) / (Dx_l + Dx_lm);
-    T r_p = (2 * Dx_l) / (Dx_l + Dx_lp);
+    T r_m = qdiv(2 * Dx_l, Dx_l + Dx_lm);
+    T r_p = qdiv(2 * Dx_l, Dx_l + Dx_lp);
     T slope_r = slope_minmod(Cm.rho, Ci.rho, Cp.rho, r_m, r_p);
     T slope_ra = slope_minmod(Cm.rua, Ci.rua, Cp.rua, r_m, r_p);
     T slope_ro = slope_minmod(Cm.ruo, Ci.ruo, Cp.ruo, r_m, r_p);
     T slope_rE = slope_minmod(Cm.rE, Ci.rE, Cp.rE, r_m, r_p);
-    T length_factor = Dx / (2 * Dx_l);
+    T length_factor = qdiv(Dx, 2 * Dx_l);
     Adv<T> a;
     a.r = disp * (Ci.rho - slope_r * length_factor);
     a.ra = disp * (Ci.rua - slope_ra * length_factor);
@@ -215,7 +233,7 @@ __device__ __forceinline__ Adv<T> advect1(const Flux<T>& Fk, const Lag<T>& Lm, c
 {
     // src/kernels/euler_projection.cpp:51-70 for face k (Lm = cell k-s, Lk = cell k)
     T disp = Fk.dtus;
-    bool up = disp > 0;
+    bool up = qgt0(disp);
     Adv<T> a;
     a.r = disp * (up ? Lm.rho : Lk.rho);
     a.ra = disp * (up ? Lm.rua : Lk.rua);
@@ -292,17 +310,28 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 CellIn<T> c;
                 bool stale = false;
                 int m = t;
-                T fa = T(1), fo = T(1);
+                int side = 0;   // 1: mirrored from the low side, 2: from the high side
                 if (t < 0) {
-                    if (t >= -sw) { m = -1 - t; fa = g.fa_lo; fo = g.fo_lo; } else stale = true;
+                    if (t >= -sw) { m = -1 - t; side = 1; } else stale = true;
                 } else if (t >= n) {
-                    if (t < n + sw) { m = 2 * n - 1 - t; fa = g.fa_hi; fo = g.fo_hi; } else stale = true;
+                    if (t < n + sw) { m = 2 * n - 1 - t; side = 2; } else stale = true;
                 }
                 const int64_t idx = base + (int64_t)m * s;
                 c.rho = rho_in[idx];
-                c.ua = apply_factor(ua_in[idx], fa);
-                c.uo = apply_factor(uo_in[idx], fo);
+                c.ua = ua_in[idx];
+                c.uo = uo_in[idx];
                 c.E = E_in[idx];
+                if (side) {
+                    // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
+                    if (g.f_unit) {
+                        const uint32_t sh = side == 1 ? 0 : 2;
+                        c.ua = qneg_if(c.ua, (g.fneg >> sh) & 1u);
+                        c.uo = qneg_if(c.uo, (g.fneg >> (sh + 1)) & 1u);
+                    } else {
+                        c.ua = c.ua * (side == 1 ? g.fa_lo : g.fa_hi);
+                        c.uo = c.uo * (side == 1 ? g.fo_lo : g.fo_hi);
+                    }
+                }
                 if (stale) {
                     c.p = A.pmat[idx];
                     c.c = A.cmat[idx];

@@ -9,6 +9,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "softfp.cuh"
+
 namespace armon {
 
 template <class T> __host__ __device__ __forceinline__ T kmin(T a, T b) { return (b < a) ? b : a; }
@@ -104,18 +106,18 @@ struct DtAcc {
         // kmax of non-negative values: for sign-clear, non-NaN doubles the IEEE order is the
         // unsigned order of the bit patterns, so the compares run on the integer pipes
         const uint64_t inf = 0x7FF0000000000000ull;
-        const uint64_t a1 = (uint64_t)__double_as_longlong(fabs(u + c));
-        const uint64_t a2 = (uint64_t)__double_as_longlong(fabs(u - c));
-        const uint64_t b1 = (uint64_t)__double_as_longlong(fabs(v + c));
-        const uint64_t b2 = (uint64_t)__double_as_longlong(fabs(v - c));
+        const uint64_t a1 = sfp::bits(sfp::absval(u + c));
+        const uint64_t a2 = sfp::bits(sfp::absval(u - c));
+        const uint64_t b1 = sfp::bits(sfp::absval(v + c));
+        const uint64_t b2 = sfp::bits(sfp::absval(v - c));
         // kmax(a1, a2) = (a1 < a2) ? a2 : a1, where a NaN a1 is kept and a NaN a2 is not taken
         const uint64_t mx = (a1 <= inf && a2 <= inf && a1 < a2) ? a2 : a1;
         const uint64_t my = (b1 <= inf && b2 <= inf && b1 < b2) ? b2 : b1;
         if (mx <= inf) {
-            const uint64_t cur = (uint64_t)__double_as_longlong(ax);
+            const uint64_t cur = sfp::bits(ax);
             if (cur < mx) ax = __longlong_as_double((long long)mx);
             if (my <= inf) {
-                const uint64_t cy = (uint64_t)__double_as_longlong(ay);
+                const uint64_t cy = sfp::bits(ay);
                 if (cy < my) ay = __longlong_as_double((long long)my);
             }
         }

@@ -111,12 +111,71 @@ __global__ void cmp_check(uint64_t seed, int64_t n, unsigned long long* out)
     }
 }
 
+__global__ void scale_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1));
+        double x = from_bits(r1);                                   // every class of operand
+        if ((r2 & 3) == 0) x = normal_double(r1, 1023);             // normal, all exponents
+        if ((r2 & 12) == 4) x = from_bits(r1 & 0x801FFFFFFFFFFFFFull);   // near the subnormal range
+        if ((r2 & 48) == 16) x = from_bits(r1 | 0x7FE0000000000000ull);  // near overflow
+        if ((r2 & 192) == 64) x = from_bits(r1 & 0x8000000000000000ull); // +-0
+        const int k = (int)((r2 >> 8) % 121) - 60;
+        const double p2 = ldexp(1.0, k);
+        const double s = scale(x, k, p2), h = x * p2;
+        bool ok = bits(s) == bits(h) || (s != s && h != h);
+        ok = ok && (bits(half(x)) == bits(x * 0.5) || x != x) && (bits(twice(x)) == bits(x * 2.0) || x != x);
+        if (!ok && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = bits(x);
+            out[3] = (uint64_t)(int64_t)k;
+        }
+    }
+}
+
+__global__ void sqrt_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1));
+        double x;
+        switch (r2 & 7) {
+        case 0: x = from_bits(r1); break;                                  // every class
+        case 1: {                                                          // exact squares
+            double q = (double)((r1 >> 38) | 1) * ldexp(1.0, (int)(r2 >> 8) % 200 - 100);
+            x = q * q;
+            break;
+        }
+        case 2: case 3: {                                                  // root near a midpoint
+            double q = normal_double(r1, 500);
+            q = fabs(q);
+            double h = q + from_bits((bits(q) & 0x7FF0000000000000ull) - (53ull << 52));   // q + ulp/2
+            x = h * h;
+            if (r2 & 8) x = from_bits(bits(x) + ((r2 >> 4) & 3) - 1);
+            break;
+        }
+        default: x = fabs(normal_double(r1, 1022)); break;                 // positive normals
+        }
+        const double s = armon::sfp::sqrt(x), h = ::sqrt(x);
+        const bool ok = bits(s) == bits(h) || (s != s && h != h);
+        const bool abs_ok = x != x || bits(absval(x)) == bits(fabs(x));
+        if (!(ok && abs_ok) && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = bits(x);
+            out[3] = bits(s);
+        }
+        // operands of the integer path: positive normals
+        if ((uint32_t)(bits(x) >> 52) - 1u < 2046u) atomicAdd(&out[1], 1ull);
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
 // mode 0..6 (see operands) checks sfp::div against the hardware quotient; mode 100 checks lt,
-// gt0 and neg_if against the IEEE comparisons.  out[0] = mismatches, out[1] = fast-path operand
+// gt0 and neg_if against the IEEE comparisons; mode 101 checks scale, half and twice against the
+// FP64 multiply by the power of two (out[3] = the exponent k of the first mismatch); mode 102
+// checks sqrt and absval against the hardware square root and fabs (out[3] = the soft root).  out[0] = mismatches, out[1] = fast-path operand
 // pairs, out[2..3] = the bits of the first mismatching operands.  Returns a cudaError_t.
 int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_host)
 {
@@ -125,6 +184,8 @@ int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_
     if (e != cudaSuccess) return (int)e;
     cudaMemset(out, 0, 4 * sizeof(unsigned long long));
     if (mode == 100) cmp_check<<<152 * 16, 256>>>(seed, n, out);
+    else if (mode == 101) scale_check<<<152 * 16, 256>>>(seed, n, out);
+    else if (mode == 102) sqrt_check<<<152 * 16, 256>>>(seed, n, out);
     else div_check<<<152 * 16, 256>>>(mode, seed, n, out);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out_host, out, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);

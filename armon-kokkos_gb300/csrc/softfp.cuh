@@ -8,7 +8,10 @@
 //   lt(x, y)      x < y  (false when either is NaN; -0 == +0)
 //   gt0(x)        x > 0
 //   neg_if(x, c)  c ? -x : x  (a sign flip: what multiplying by -1 gives for non-NaN x)
+//   scale(x, k)   x * 2^k, exact (half(x) = x * 0.5, twice(x) = x * 2)
+//   absval(x)     |x|
 //   div(a, b)     the correctly rounded quotient (round to nearest, ties to even)
+//   sqrt(x)       the correctly rounded square root
 //
 // Division (my own construction from the arithmetic, not a library's sequence).  With
 // significands ma, mb in [2^52, 2^53) and ma doubled when ma < mb, the result significand is
@@ -28,7 +31,15 @@
 namespace armon {
 namespace sfp {
 
-__device__ __forceinline__ uint64_t bits(double x) { return (uint64_t)__double_as_longlong(x); }
+// The bit pattern is taken in inline PTX so that the compiler cannot see the integer tests that
+// follow as floating-point class tests (zero, NaN, normal), which it would otherwise fold back into
+// FP64 compares on the FP64 pipe.
+__device__ __forceinline__ uint64_t bits(double x)
+{
+    uint64_t u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
+}
 __device__ __forceinline__ double from_bits(uint64_t u) { return __longlong_as_double((long long)u); }
 
 constexpr uint64_t kAbs = 0x7FFFFFFFFFFFFFFFull;
@@ -56,10 +67,38 @@ __device__ __forceinline__ bool gt0(double x)
     return u > 0 && (uint64_t)u <= kInf;
 }
 
+// The sign-bit operations are written on the high word in inline PTX: a plain xor / and of the
+// bit pattern is recognised as an FP negation / absolute value, which can be materialised on the
+// FP64 pipe.
 __device__ __forceinline__ double neg_if(double x, bool c)
 {
-    return from_bits(bits(x) ^ ((uint64_t)c << 63));
+    const uint32_t m = (uint32_t)c << 31;
+    uint32_t hi;
+    asm("xor.b32 %0, %1, %2;" : "=r"(hi) : "r"((uint32_t)__double2hiint(x)), "r"(m));
+    return __hiloint2double((int)hi, __double2loint(x));
 }
+
+__device__ __forceinline__ double absval(double x)
+{
+    uint32_t hi;
+    asm("and.b32 %0, %1, 0x7FFFFFFF;" : "=r"(hi) : "r"((uint32_t)__double2hiint(x)));
+    return __hiloint2double((int)hi, __double2loint(x));
+}
+
+// x * 2^k for |k| < 2046: exact whenever x and the result are normal, so the exponent field moves
+// by k; zeros are returned as they are; everything else (subnormal operand or result, overflow,
+// infinities, NaN) takes the FP64 multiply by the power of two `p2` (== 2^k).
+__device__ __forceinline__ double scale(double x, int k, double p2)
+{
+    const uint64_t u = bits(x);
+    const int e = (int)((u >> 52) & 0x7FFu);
+    if ((unsigned)(e - 1) < 2046u && (unsigned)(e + k - 1) < 2046u)
+        return from_bits(u + ((uint64_t)(int64_t)k << 52));
+    if ((u << 1) == 0) return x;
+    return x * p2;
+}
+__device__ __forceinline__ double half(double x) { return scale(x, -1, 0.5); }
+__device__ __forceinline__ double twice(double x) { return scale(x, 1, 2.0); }
 
 __device__ __forceinline__ double div(double a, double b)
 {
@@ -126,6 +165,59 @@ __device__ __forceinline__ double div(double a, double b)
     const bool up = r2 > mb || (r2 == mb && (q & 1));
     q += up ? 1ull : 0ull;
     return from_bits(sign + ((uint64_t)(e + 1022) << 52) + q);
+}
+
+// Square root (my own construction, in the manner of the division above).  A positive normal
+// x = m 2^(e-1075), m in [2^52, 2^53), has its significand doubled when e - 1075 is odd, giving
+// M = m 2^odd in [2^52, 2^54) over an even exponent.  The result significand is
+// Q = floor(sqrt(M 2^52)) in [2^52, 2^53), rounded up when the remainder R = M 2^52 - Q^2 exceeds
+// Q (a square root is never exactly halfway between two doubles, so there are no ties).  Q is
+// estimated from y ~ 1/sqrt(a), a = M / 2^52 in [1, 4): an FP32 seed (rsqrt.approx of the top
+// 24 bits of a), two Newton steps y <- y + y (1 - a y^2) / 2 in 64-bit fixed point, then
+// g = a y.  The estimate, lowered by one, is corrected on the exact remainder (computed modulo
+// 2^64, exact because |R| < 2^58 for an estimate within a few units); if R is still outside
+// [0, 2Q] the hardware square root is used.  Zeros are returned as they are; negative, subnormal,
+// infinite and NaN operands take the hardware square root.
+__device__ __forceinline__ double sqrt(double x)
+{
+    const uint64_t u = bits(x);
+    const uint32_t e = (uint32_t)(u >> 52);                  // sign and exponent
+    if (e - 1u >= 2046u) return (u << 1) == 0 ? x : ::sqrt(x);
+    const uint32_t odd = (e & 1u) ^ 1u;                      // e - 1075 is odd
+    const uint64_t M = ((u & kMant) | kHidden) << odd;       // [2^52, 2^54)
+    const uint64_t A = M << 10;                              // a in Q62
+    const uint32_t fa = ((127u + odd) << 23) | ((uint32_t)(M >> (29 + odd)) & 0x7FFFFFu);   // a, truncated
+    float rf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fa)));
+    const uint32_t ur = __float_as_uint(rf);
+    const uint32_t er = ur >> 23;
+    int64_t Y;                                               // y in Q62, in [2^61, 2^62]
+    if (er >= 127u) Y = 1ll << 62;
+    else if (er < 126u) Y = 1ll << 61;
+    else Y = (int64_t)((ur & 0x7FFFFFu) | 0x800000u) << 38;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const uint64_t y2 = __umul64hi((uint64_t)Y, (uint64_t)Y);   // y^2 in Q60
+        const uint64_t ay2 = __umul64hi(A, y2);                     // a y^2 in Q58
+        const int64_t err = (int64_t)((1ull << 58) - ay2);          // 1 - a y^2 in Q58
+        Y += __mul64hi(Y, err) << 5;                                // + y (1 - a y^2) / 2
+    }
+    uint64_t Q = (__umul64hi(A, (uint64_t)Y) >> 8) - 1;             // g = a y in Q60, to Q52
+    int64_t R = (int64_t)((M << 52) - Q * Q);
+    if (R < 0) {
+        Q -= 1;
+        R += (int64_t)(2 * Q + 1);
+    }
+#pragma unroll
+    for (int it = 0; it < 3; it++) {
+        const bool up = R > (int64_t)(2 * Q);
+        R -= up ? (int64_t)(2 * Q + 1) : 0;
+        Q += up ? 1u : 0u;
+    }
+    if (R < 0 || R > (int64_t)(2 * Q)) return ::sqrt(x);   // outside the error bounds
+    Q += R > (int64_t)Q ? 1u : 0u;
+    const int be = ((int)e - 1075 - (int)odd) / 2 + 1049;          // biased exponent of the result
+    return from_bits(((uint64_t)(be - 1) << 52) + Q);
 }
 
 }  // namespace sfp

@@ -128,6 +128,7 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, int fo
         g.dx = T(dx);
         g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;
         g.inv_dx = g.dx_pow2 ? T(1.0 / double(g.dx)) : T(0);
+        g.dx_log2 = g.dx_pow2 ? std::ilogb(double(g.dx)) : 0;
     }
     a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
     a.sw = p.stencil_width;

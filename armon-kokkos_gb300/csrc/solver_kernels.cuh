@@ -125,7 +125,7 @@ __global__ void conservation_partial_kernel(ConsArgs a)
     }
 }
 
-__global__ inline void conservation_final_kernel(const double* partials, int n, double* out)
+static __global__ void conservation_final_kernel(const double* partials, int n, double* out)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double m = 0, e = 0;

@@ -20,8 +20,10 @@
 //
 // Exactness.  Every value is computed with the reference's expression tree; the file is compiled
 // with --fmad=false, so results are bit-identical to the reference's strict build.  Reuse only
-// replaces a recomputation of the same expression on the same inputs.  Division by dx becomes a
-// multiplication only when dx is a power of two (then both are exact scalings).
+// replaces a recomputation of the same expression on the same inputs (differences of adjacent
+// cells or faces, rho c, rho dx, width sums, which IEEE addition's commutativity makes shareable).
+// Division by dx becomes a multiplication only when dx is a power of two (then both are exact
+// scalings); exact scalings by powers of two move the exponent field on the integer pipes.
 //
 // Ghosts.  Positions -sw..-1 and n..n+sw-1 are the mirror images of real cells with the sign
 // factors of the side (what boundary_conditions writes); EOS of a mirrored state equals the copied
@@ -58,7 +60,7 @@ struct AxisGeom {
     int32_t dx_pow2;
     uint32_t fneg;      // bit k set: factor k (fa_lo, fo_lo, fa_hi, fo_hi) is -1
     int32_t f_unit;     // every factor is +1 or -1: apply them as sign flips
-    int32_t pad;
+    int32_t dx_log2;    // dx == 2^dx_log2 when dx_pow2
 };
 
 template <class T>
@@ -79,11 +81,15 @@ struct SweepArgs {
     double* partials;                 // 2 doubles per block (dt reduction)
 };
 
-template <class T> struct CellIn { T rho, ua, uo, E, p, c; };
+// rc = rho c, rcu = rc ua, dm = rho dx: the products that the two faces of a cell both use
+template <class T> struct CellIn { T rho, ua, uo, E, p, c, rc, rcu, dm; };
 template <class T> struct God { T us, ps, rcs; };            // rcs = rho_l c_l + rho_r c_r
 template <class T> struct Flux { T us, ps, psus, dtus; };    // psus = p* u*, dtus = dt u*
 template <class T> struct Lag { T rho, ua, uo, E, rua, ruo, rE, W, c; };
 template <class T> struct Adv { T r, ra, ro, rE; };
+// Differences of the Godunov state across a face g (between cells g-1 and g), each used by the
+// GAD fluxes of two faces: a = u*_g - u_{g-1}, b = u_g - u*_g, and the same for p.
+template <class T> struct GadDiff { T au, bu, ap, bp; };
 
 // Operations that the FP64 pass routes to the integer pipes (softfp.cuh: GB300's FP64 pipe is the
 // bottleneck, its integer and FP32 pipes are idle) and the FP32 pass keeps on the FP32 pipe.  Both
@@ -98,6 +104,15 @@ __device__ __forceinline__ double qneg_if(double x, bool c) { return ARMON_SOFT_
 __device__ __forceinline__ float qneg_if(float x, bool c) { return c ? -x : x; }
 __device__ __forceinline__ bool qsignbit(double x) { return (int64_t)sfp::bits(x) < 0; }
 __device__ __forceinline__ bool qsignbit(float x) { return (int32_t)__float_as_uint(x) < 0; }
+// exact scalings: x * 0.5, x * 2, x * 2^k (p2 == 2^k)
+__device__ __forceinline__ double qhalf(double x) { return ARMON_SOFT_FP64 ? sfp::half(x) : x * 0.5; }
+__device__ __forceinline__ float qhalf(float x) { return x * 0.5f; }
+__device__ __forceinline__ double qtwice(double x) { return ARMON_SOFT_FP64 ? sfp::twice(x) : x * 2.0; }
+__device__ __forceinline__ float qtwice(float x) { return x * 2.0f; }
+__device__ __forceinline__ double qscale(double x, int k, double p2) { return ARMON_SOFT_FP64 ? sfp::scale(x, k, p2) : x * p2; }
+__device__ __forceinline__ float qscale(float x, int, float p2) { return x * p2; }
+__device__ __forceinline__ double qsqrt(double x) { return ARMON_SOFT_FP64 ? sfp::sqrt(x) : ::sqrt(x); }
+__device__ __forceinline__ float qsqrt(float x) { return sqrtf(x); }
 // Kokkos::min / Kokkos::max: (b < a) ? b : a and (a < b) ? b : a
 template <class T> __device__ __forceinline__ T qmin(T a, T b) { return qlt(b, a) ? b : a; }
 template <class T> __device__ __forceinline__ T qmax(T a, T b) { return qlt(a, b) ? b : a; }
@@ -107,17 +122,19 @@ __device__ __forceinline__ T limiter_fn(int L, T r)
 {
     // src/kernels/limiters.h:15-34
     if (L == 1) return qmax(T(0), qmin(T(1), r));
-    if (L == 2) return qmax(qmax(T(0), qmin(T(1), 2 * r)), qmin(T(2), r));
+    if (L == 2) return qmax(qmax(T(0), qmin(T(1), qtwice(r))), qmin(T(2), r));
     return T(1);
 }
 
 template <class T>
-__device__ __forceinline__ T slope_minmod(T u_im, T u_i, T u_ip, T r_m, T r_p)
+__device__ __forceinline__ T slope_minmod(T d_m, T d_p, T r_m, T r_p)
 {
-    // src/kernels/euler_projection.cpp:73-79.  s = copysign(1, D_u_p) is +-1, so s * v is v with
-    // its sign flipped when D_u_p's sign bit is set (bit-identical to the multiply for non-NaN v).
-    T D_u_p = r_p * (u_ip - u_i);
-    T D_u_m = r_m * (u_i - u_im);
+    // src/kernels/euler_projection.cpp:73-79 with d_p = u_ip - u_i and d_m = u_i - u_im (the
+    // differences of adjacent cells, shared by neighbouring faces).  s = copysign(1, D_u_p) is
+    // +-1, so s * v is v with its sign flipped when D_u_p's sign bit is set (bit-identical to the
+    // multiply for non-NaN v).
+    T D_u_p = r_p * d_p;
+    T D_u_m = r_m * d_m;
     const bool neg = qsignbit(D_u_p);
     return qneg_if(qmax(T(0), qmin(qneg_if(D_u_p, neg), qneg_if(D_u_m, neg))), neg);
 }
@@ -125,51 +142,66 @@ __device__ __forceinline__ T slope_minmod(T u_im, T u_i, T u_ip, T r_m, T r_p)
 template <class T>
 __device__ __forceinline__ T div_dx(T x, const AxisGeom<T>& g)
 {
-    return g.dx_pow2 ? x * g.inv_dx : qdiv(x, g.dx);
+    return g.dx_pow2 ? qscale(x, -g.dx_log2, g.inv_dx) : qdiv(x, g.dx);
 }
 
 template <class T>
-__device__ __forceinline__ void eos(CellIn<T>& c, T gamma)
+__device__ __forceinline__ T mul_dx(T x, const AxisGeom<T>& g)
 {
-    // src/kernels/fluid_eos.cpp:18-21
-    T e = c.E - T(0.5) * (c.ua * c.ua + c.uo * c.uo);
-    c.p = (gamma - 1) * c.rho * e;
-    c.c = sqrt(qdiv(gamma * c.p, c.rho));
+    return g.dx_pow2 ? qscale(x, g.dx_log2, g.dx) : x * g.dx;
+}
+
+template <class T>
+__device__ __forceinline__ void eos(CellIn<T>& c, T gamma, T gamma_m1)
+{
+    // src/kernels/fluid_eos.cpp:18-21 (gamma_m1 = gamma - 1, computed once)
+    T e = c.E - qhalf(c.ua * c.ua + c.uo * c.uo);
+    c.p = gamma_m1 * c.rho * e;
+    c.c = qsqrt(qdiv(gamma * c.p, c.rho));
 }
 
 template <class T>
 __device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R)
 {
-    // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i)
+    // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i); rc_l * L.ua == L.rcu
     God<T> g;
-    T rc_l = L.rho * L.c;
-    T rc_r = R.rho * R.c;
-    g.rcs = rc_l + rc_r;
-    g.us = qdiv(rc_l * L.ua + rc_r * R.ua + (L.p - R.p), g.rcs);
-    g.ps = qdiv(rc_r * L.p + rc_l * R.p + rc_l * rc_r * (L.ua - R.ua), g.rcs);
+    g.rcs = L.rc + R.rc;
+    g.us = qdiv(L.rcu + R.rcu + (L.p - R.p), g.rcs);
+    g.ps = qdiv(R.rc * L.p + L.rc * R.p + L.rc * R.rc * (L.ua - R.ua), g.rcs);
     return g;
 }
 
 template <class T>
-__device__ __forceinline__ Flux<T> gad(const God<T>& Gm, const God<T>& Gc, const God<T>& Gp,
-                                       const CellIn<T>& Cl, const CellIn<T>& Cr, int L, T dt, T dx)
+__device__ __forceinline__ GadDiff<T> gad_diff(const God<T>& G, const CellIn<T>& Cl, const CellIn<T>& Cr)
 {
-    // src/kernels/acoustic.cpp:40-88 (face between Cl = i-s and Cr = i)
-    T r_um = qdiv(Gp.us - Cr.ua, Gc.us - Cl.ua + T(1e-6));
-    T r_pm = qdiv(Gp.ps - Cr.p, Gc.ps - Cl.p + T(1e-6));
-    T r_up = qdiv(Cl.ua - Gm.us, Cr.ua - Gc.us + T(1e-6));
-    T r_pp = qdiv(Cl.p - Gm.ps, Cr.p - Gc.ps + T(1e-6));
+    GadDiff<T> d;
+    d.au = G.us - Cl.ua;
+    d.bu = Cr.ua - G.us;
+    d.ap = G.ps - Cl.p;
+    d.bp = Cr.p - G.ps;
+    return d;
+}
+
+template <class T>
+__device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, const GadDiff<T>& D0,
+                                       const GadDiff<T>& Dp1, T dm_l, T dm_r, int L, T dt)
+{
+    // src/kernels/acoustic.cpp:40-88 for face i (between cells i-s and i), with the differences
+    // of faces i-s (Dm1), i (D0), i+s (Dp1):  Gp.us - Cr.ua == Dp1.au, Gc.us - Cl.ua == D0.au,
+    // Cl.ua - Gm.us == Dm1.bu, Cr.ua - Gc.us == D0.bu (the same for p).
+    T r_um = qdiv(Dp1.au, D0.au + T(1e-6));
+    T r_pm = qdiv(Dp1.ap, D0.ap + T(1e-6));
+    T r_up = qdiv(Dm1.bu, D0.bu + T(1e-6));
+    T r_pp = qdiv(Dm1.bp, D0.bp + T(1e-6));
     r_um = limiter_fn(L, r_um);
     r_pm = limiter_fn(L, r_pm);
     r_up = limiter_fn(L, r_up);
     r_pp = limiter_fn(L, r_pp);
-    T dm_l = Cl.rho * dx;
-    T dm_r = Cr.rho * dx;
-    T Dm = (dm_l + dm_r) * T(0.5);                       // (dm_l + dm_r) / 2
-    T theta = T(0.5) * (1 - (Gc.rcs * T(0.5)) * qdiv(dt, Dm));
+    T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
+    T theta = qhalf(1 - qhalf(Gc.rcs) * qdiv(dt, Dm));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
-    f.us = Gc.us + theta * (r_up * (Cr.ua - Gc.us) - r_um * (Gc.us - Cl.ua));
-    f.ps = Gc.ps + theta * (r_pp * (Cr.p - Gc.ps) - r_pm * (Gc.ps - Cl.p));
+    f.us = Gc.us + theta * (r_up * D0.bu - r_um * D0.au);
+    f.ps = Gc.ps + theta * (r_pp * D0.bp - r_pm * D0.ap);
     return f;
 }
 
@@ -178,7 +210,7 @@ __device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0
 {
     // src/kernels/euler_projection.cpp:9-22 for cell i (F0 = face i, F1 = face i+s)
     Lag<T> l;
-    T dm = C.rho * dx;
+    const T dm = C.dm;
     l.W = dx + dt * (F1.us - F0.us);
     l.rho = qdiv(dm, l.W);
     T dtdm = qdiv(dt, dm);
@@ -192,39 +224,40 @@ __device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0
     return l;
 }
 
+// The advected quantities of a Lagrangian cell, and differences of adjacent cells' ones.
 template <class T>
-__device__ __forceinline__ Lag<T> sel(bool p, const Lag<T>& a, const Lag<T>& b)
+__device__ __forceinline__ Adv<T> lag_diff(const Lag<T>& lo, const Lag<T>& hi)
 {
-    Lag<T> r;
-    r.rho = p ? a.rho : b.rho; r.ua = p ? a.ua : b.ua; r.uo = p ? a.uo : b.uo; r.E = p ? a.E : b.E;
-    r.rua = p ? a.rua : b.rua; r.ruo = p ? a.ruo : b.ruo; r.rE = p ? a.rE : b.rE;
-    r.W = p ? a.W : b.W; r.c = p ? a.c : b.c;
-    return r;
+    return Adv<T>{hi.rho - lo.rho, hi.rua - lo.rua, hi.ruo - lo.ruo, hi.rE - lo.rE};
 }
 
 template <class T>
 __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, const Flux<T>& Fp,
-                                          const Lag<T>& L0, const Lag<T>& L1, const Lag<T>& L2, const Lag<T>& L3,
-                                          T dx)
+                                          const Lag<T>& L1, const Lag<T>& L2, const Adv<T>& d01,
+                                          const Adv<T>& d12, const Adv<T>& d23, T s01, T s12, T s23, T dx)
 {
-    // src/kernels/euler_projection.cpp:82-120 for face k; L0..L3 = cells k-2..k+1
+    // src/kernels/euler_projection.cpp:82-120 for face k, from cells L1 = k-1 and L2 = k and the
+    // differences d01 = L(k-1) - L(k-2), d12 = L(k) - L(k-1), d23 = L(k+1) - L(k), and the width
+    // sums s01 = W(k-2) + W(k-1), s12, s23, which neighbouring faces share.  Upwind (disp > 0) the
+    // cells are (k-2, k-1, k), else (k-1, k, k+1).  x + y == y + x exactly, and
+    // -(dx - y) == -(dx + (-y)), so the face's Dx costs one addition.
     T disp = Fk.dtus;
     bool up = qgt0(disp);
-    T Dx = up ? -(dx - Fm.dtus) : dx + Fp.dtus;
-    Lag<T> Cm = sel(up, L0, L1), Ci = sel(up, L1, L2), Cp = sel(up, L2, L3);
-    T Dx_lm = Cm.W, Dx_l = Ci.W, Dx_lp = Cp.W;
-    T r_m = qdiv(2 * Dx_l, Dx_l + Dx_lm);
-    T r_p = qdiv(2 * Dx_l, Dx_l + Dx_lp);
-    T slope_r = slope_minmod(Cm.rho, Ci.rho, Cp.rho, r_m, r_p);
-    T slope_ra = slope_minmod(Cm.rua, Ci.rua, Cp.rua, r_m, r_p);
-    T slope_ro = slope_minmod(Cm.ruo, Ci.ruo, Cp.ruo, r_m, r_p);
-    T slope_rE = slope_minmod(Cm.rE, Ci.rE, Cp.rE, r_m, r_p);
-    T length_factor = qdiv(Dx, 2 * Dx_l);
+    T Dx = qneg_if(dx + (up ? qneg_if(Fm.dtus, true) : Fp.dtus), up);
+    const T Dx_l = up ? L1.W : L2.W;
+    const T two_Dx_l = qtwice(Dx_l);
+    T r_m = qdiv(two_Dx_l, up ? s01 : s12);    // 2 Dx_l / (Dx_l + Dx_lm)
+    T r_p = qdiv(two_Dx_l, up ? s12 : s23);    // 2 Dx_l / (Dx_l + Dx_lp)
+    T slope_r = slope_minmod(up ? d01.r : d12.r, up ? d12.r : d23.r, r_m, r_p);
+    T slope_ra = slope_minmod(up ? d01.ra : d12.ra, up ? d12.ra : d23.ra, r_m, r_p);
+    T slope_ro = slope_minmod(up ? d01.ro : d12.ro, up ? d12.ro : d23.ro, r_m, r_p);
+    T slope_rE = slope_minmod(up ? d01.rE : d12.rE, up ? d12.rE : d23.rE, r_m, r_p);
+    T length_factor = qdiv(Dx, two_Dx_l);
     Adv<T> a;
-    a.r = disp * (Ci.rho - slope_r * length_factor);
-    a.ra = disp * (Ci.rua - slope_ra * length_factor);
-    a.ro = disp * (Ci.ruo - slope_ro * length_factor);
-    a.rE = disp * (Ci.rE - slope_rE * length_factor);
+    a.r = disp * ((up ? L1.rho : L2.rho) - slope_r * length_factor);
+    a.ra = disp * ((up ? L1.rua : L2.rua) - slope_ra * length_factor);
+    a.ro = disp * ((up ? L1.ruo : L2.ruo) - slope_ro * length_factor);
+    a.rE = disp * ((up ? L1.rE : L2.rE) - slope_rE * length_factor);
     return a;
 }
 
@@ -242,164 +275,14 @@ __device__ __forceinline__ Adv<T> advect1(const Flux<T>& Fk, const Lag<T>& Lm, c
     return a;
 }
 
-// One axis pass of one domain, as block `blk` of the `nblk` blocks given to that domain.
-// Scheme 0 Godunov / 1 GAD; Proj 1 first order / 2 second order; LAST: the pass that ends a cycle.
-template <class T, int SCHEME, int PROJ, bool LAST>
-__device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int blk, const int nblk, const int pass)
+// The end of the last pass of a cycle: the block reduction of the dt maxima, then the last block to
+// finish commits dt_CFL, time and cycle to the step state.
+template <class T>
+__device__ __forceinline__ void commit_cycle(const SweepArgs<T>& A, DtAcc acc, const StepState& st,
+                                             const CycleDt& cd, const int blk, const int nblk)
 {
-    constexpr bool kGAD = SCHEME == 1;
-    constexpr bool kE2 = PROJ == 2;
-    constexpr int LAG_F = kGAD ? 1 : 0;             // flux face = t - LAG_F
-    constexpr int LAG_L = LAG_F + 1;                // Lagrange cell
-    constexpr int LAG_A = kE2 ? LAG_F + 2 : LAG_L;  // advection face
-    constexpr int H = LAG_A + 1;                    // projection lag == stencil reach
-
     __shared__ double red[2][4];
     __shared__ int is_last_block;
-
-    const StepState st = *A.state;
-    const CycleDt cd = cycle_time_step(st, A.cfg);
-    if (!cd.run) return;
-    if (cd.invalid) {
-        if (LAST && blk == 0 && threadIdx.x == 0) A.state->status = STATUS_INVALID_DT;
-        return;
-    }
-
-    int axis;
-    double factor;
-    split_axis(A.cfg.splitting, st.cycle, pass, &axis, &factor);
-    const AxisGeom<T>& g = A.geom[axis];
-    const T dt = T(cd.current * factor);
-    const T dx = g.dx;
-    const int src = (int)(((int64_t)st.cycle * A.npass + pass + st.buf_base) & 1);
-    T* const* in = A.buf[src];
-    T* const* out = A.buf[src ^ 1];
-    // X pass: the axis velocity is umat (1), Y pass: vmat (2)
-    const T* __restrict__ rho_in = in[0];
-    const T* __restrict__ ua_in = in[axis == 0 ? 1 : 2];
-    const T* __restrict__ uo_in = in[axis == 0 ? 2 : 1];
-    const T* __restrict__ E_in = in[3];
-
-    DtAcc acc;
-    acc.init();
-
-    const int lb = blk % max(g.nlb, 1);
-    const int seg = blk / max(g.nlb, 1);
-    const int line = lb * blockDim.x + threadIdx.x;
-    const bool active = blk < g.blocks && line < g.nlines;
-
-    if (active) {
-        const int n = g.n, sw = A.sw;
-        const int a0 = seg * g.seg_len;
-        const int b0 = min(n, a0 + g.seg_len);
-        const int64_t base = A.origin + (int64_t)line * g.lstride;
-        const int64_t s = g.s;
-        const int t0 = a0 - H, t1 = b0 - 1 + H;
-        const int firstF = kGAD ? t0 + 2 : t0 + 1;
-
-        CellIn<T> C0{}, C1{}, C2{};
-        God<T> G0{}, G1{}, G2{};
-        Flux<T> F0{}, F1{}, F2{}, F3{}, F4{};
-        Lag<T> L0{}, L1{}, L2{}, L3{};
-        Adv<T> A0{}, A1{};
-
-        for (int t = t0; t <= t1; ++t) {
-            // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
-            C0 = C1; C1 = C2;
-            {
-                CellIn<T> c;
-                bool stale = false;
-                int m = t;
-                int side = 0;   // 1: mirrored from the low side, 2: from the high side
-                if (t < 0) {
-                    if (t >= -sw) { m = -1 - t; side = 1; } else stale = true;
-                } else if (t >= n) {
-                    if (t < n + sw) { m = 2 * n - 1 - t; side = 2; } else stale = true;
-                }
-                const int64_t idx = base + (int64_t)m * s;
-                c.rho = rho_in[idx];
-                c.ua = ua_in[idx];
-                c.uo = uo_in[idx];
-                c.E = E_in[idx];
-                if (side) {
-                    // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
-                    if (g.f_unit) {
-                        const uint32_t sh = side == 1 ? 0 : 2;
-                        c.ua = qneg_if(c.ua, (g.fneg >> sh) & 1u);
-                        c.uo = qneg_if(c.uo, (g.fneg >> (sh + 1)) & 1u);
-                    } else {
-                        c.ua = c.ua * (side == 1 ? g.fa_lo : g.fa_hi);
-                        c.uo = c.uo * (side == 1 ? g.fo_lo : g.fo_hi);
-                    }
-                }
-                if (stale) {
-                    c.p = A.pmat[idx];
-                    c.c = A.cmat[idx];
-                } else {
-                    eos(c, A.gamma);
-                    if (m == t && t >= a0 && t < b0 && A.write_eos) {   // owned real cell: what update_EOS stores
-                        A.pmat[idx] = c.p;
-                        A.cmat[idx] = c.c;
-                        A.gmat[idx] = (1 + A.gamma) / 2;
-                    }
-                }
-                C2 = c;
-            }
-            // ---- Godunov face t ----
-            if (t >= t0 + 1) { G0 = G1; G1 = G2; G2 = godunov(C1, C2); }
-            // ---- numerical flux at face f = t - LAG_F ----
-            if (kGAD ? (t >= t0 + 3) : (t >= t0 + 1)) {
-                F0 = F1; F1 = F2; F2 = F3; F3 = F4;
-                Flux<T> f;
-                if (kGAD) {
-                    f = gad(G0, G1, G2, C0, C1, A.limiter, dt, dx);
-                } else {
-                    f.us = G2.us; f.ps = G2.ps;
-                }
-                f.psus = f.ps * f.us;
-                f.dtus = dt * f.us;
-                F4 = f;
-            }
-            // ---- Lagrange update of cell j = t - LAG_L ----
-            const int j = t - LAG_L;
-            if (j >= firstF) {
-                L0 = L1; L1 = L2; L2 = L3;
-                L3 = lagrange(kGAD ? C0 : C1, F3, F4, dt, dx);
-            }
-            // ---- advection flux at face k = t - LAG_A ----
-            const int k = t - LAG_A;
-            if (k >= a0) {
-                A0 = A1;
-                A1 = kE2 ? advect2(F1, F2, F3, L0, L1, L2, L3, dx) : advect1(F3, L2, L3);
-            }
-            // ---- projection of cell mm = k - 1 ----
-            const int mm = k - 1;
-            if (mm >= a0) {
-                const Lag<T>& Lc = kE2 ? L1 : L2;
-                // src/kernels/euler_projection.cpp:36-46
-                T dXr = Lc.W * Lc.rho;
-                T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
-                T tmp_ra = div_dx(dXr * Lc.ua - (A1.ra - A0.ra), g);
-                T tmp_ro = div_dx(dXr * Lc.uo - (A1.ro - A0.ro), g);
-                T tmp_rE = div_dx(dXr * Lc.E - (A1.rE - A0.rE), g);
-                T ua = tmp_ra / tmp_rho, uo = tmp_ro / tmp_rho, E = tmp_rE / tmp_rho;
-                const int64_t idx = base + (int64_t)mm * s;
-                out[0][idx] = tmp_rho;
-                out[axis == 0 ? 1 : 2][idx] = ua;
-                out[axis == 0 ? 2 : 1][idx] = uo;
-                out[3][idx] = E;
-                if (LAST) {
-                    // dt_CFL of the state after this pass, with c from this pass's EOS
-                    if (axis == 0) acc.add(ua, uo, Lc.c);
-                    else acc.add(uo, ua, Lc.c);
-                }
-            }
-        }
-    }
-
-    if (!LAST) return;
-
-    // ---- block reduction of the dt maxima, then the last block commits the cycle ----
     for (int o = 16; o > 0; o >>= 1) {
         acc.merge(__shfl_xor_sync(0xffffffffu, acc.ax, o), __shfl_xor_sync(0xffffffffu, acc.ay, o));
     }
@@ -439,6 +322,176 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         ns.counter = 0;
         *A.state = ns;
     }
+}
+
+// One axis pass of one domain, as block `blk` of the `nblk` blocks given to that domain.
+// Scheme 0 Godunov / 1 GAD; Proj 1 first order / 2 second order; LAST: the pass that ends a cycle.
+template <class T, int SCHEME, int PROJ, bool LAST>
+__device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int blk, const int nblk, const int pass)
+{
+    constexpr bool kGAD = SCHEME == 1;
+    constexpr bool kE2 = PROJ == 2;
+    constexpr int LAG_F = kGAD ? 1 : 0;             // flux face = t - LAG_F
+    constexpr int LAG_L = LAG_F + 1;                // Lagrange cell
+    constexpr int LAG_A = kE2 ? LAG_F + 2 : LAG_L;  // advection face
+    constexpr int H = LAG_A + 1;                    // projection lag == stencil reach
+
+    const StepState st = *A.state;
+    const CycleDt cd = cycle_time_step(st, A.cfg);
+    if (!cd.run) return;
+    if (cd.invalid) {
+        if (LAST && blk == 0 && threadIdx.x == 0) A.state->status = STATUS_INVALID_DT;
+        return;
+    }
+
+    int axis;
+    double factor;
+    split_axis(A.cfg.splitting, st.cycle, pass, &axis, &factor);
+    const AxisGeom<T>& g = A.geom[axis];
+    const T dt = T(cd.current * factor);
+    const T dx = g.dx;
+    const int src = (int)(((int64_t)st.cycle * A.npass + pass + st.buf_base) & 1);
+    T* const* in = A.buf[src];
+    T* const* out = A.buf[src ^ 1];
+    // X pass: the axis velocity is umat (1), Y pass: vmat (2)
+    const T* __restrict__ rho_in = in[0];
+    const T* __restrict__ ua_in = in[axis == 0 ? 1 : 2];
+    const T* __restrict__ uo_in = in[axis == 0 ? 2 : 1];
+    const T* __restrict__ E_in = in[3];
+
+    DtAcc acc;
+    acc.init();
+    const T gamma_m1 = A.gamma - 1;
+
+    const int lb = blk % max(g.nlb, 1);
+    const int seg = blk / max(g.nlb, 1);
+    const int line = lb * blockDim.x + threadIdx.x;
+    const bool active = blk < g.blocks && line < g.nlines;
+
+    if (active) {
+        const int n = g.n, sw = A.sw;
+        const int a0 = seg * g.seg_len;
+        const int b0 = min(n, a0 + g.seg_len);
+        const int64_t base = A.origin + (int64_t)line * g.lstride;
+        const int64_t s = g.s;
+        const int t0 = a0 - H, t1 = b0 - 1 + H;
+        const int firstF = kGAD ? t0 + 2 : t0 + 1;
+
+        CellIn<T> C0{}, C1{}, C2{};
+        God<T> G1{}, G2{};
+        GadDiff<T> D0{}, D1{}, D2{};         // faces t-2, t-1, t
+        Flux<T> F0{}, F1{}, F2{}, F3{}, F4{};
+        Lag<T> L1{}, L2{}, L3{};
+        Adv<T> d01{}, d12{}, d23{};          // L(j+1) - L(j) for the Lagrangian cells
+        T s01{}, s12{}, s23{};               // W(j) + W(j+1)
+        Adv<T> A0{}, A1{};
+
+        for (int t = t0; t <= t1; ++t) {
+            // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
+            C0 = C1; C1 = C2;
+            {
+                CellIn<T> c;
+                bool stale = false;
+                int m = t;
+                int side = 0;   // 1: mirrored from the low side, 2: from the high side
+                if (t < 0) {
+                    if (t >= -sw) { m = -1 - t; side = 1; } else stale = true;
+                } else if (t >= n) {
+                    if (t < n + sw) { m = 2 * n - 1 - t; side = 2; } else stale = true;
+                }
+                const int64_t idx = base + (int64_t)m * s;
+                c.rho = rho_in[idx];
+                c.ua = ua_in[idx];
+                c.uo = uo_in[idx];
+                c.E = E_in[idx];
+                if (side) {
+                    // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
+                    if (g.f_unit) {
+                        const uint32_t sh = side == 1 ? 0 : 2;
+                        c.ua = qneg_if(c.ua, (g.fneg >> sh) & 1u);
+                        c.uo = qneg_if(c.uo, (g.fneg >> (sh + 1)) & 1u);
+                    } else {
+                        c.ua = c.ua * (side == 1 ? g.fa_lo : g.fa_hi);
+                        c.uo = c.uo * (side == 1 ? g.fo_lo : g.fo_hi);
+                    }
+                }
+                if (stale) {
+                    c.p = A.pmat[idx];
+                    c.c = A.cmat[idx];
+                } else {
+                    eos(c, A.gamma, gamma_m1);
+                    if (m == t && t >= a0 && t < b0 && A.write_eos) {   // owned real cell: what update_EOS stores
+                        A.pmat[idx] = c.p;
+                        A.cmat[idx] = c.c;
+                        A.gmat[idx] = (1 + A.gamma) / 2;
+                    }
+                }
+                c.rc = c.rho * c.c;
+                c.rcu = c.rc * c.ua;
+                c.dm = mul_dx(c.rho, g);
+                C2 = c;
+            }
+            // ---- Godunov face t ----
+            if (t >= t0 + 1) {
+                G1 = G2;
+                G2 = godunov(C1, C2);
+                if (kGAD) { D0 = D1; D1 = D2; D2 = gad_diff(G2, C1, C2); }
+            }
+            // ---- numerical flux at face f = t - LAG_F ----
+            if (kGAD ? (t >= t0 + 3) : (t >= t0 + 1)) {
+                F0 = F1; F1 = F2; F2 = F3; F3 = F4;
+                Flux<T> f;
+                if (kGAD) {
+                    f = gad(G1, D0, D1, D2, C0.dm, C1.dm, A.limiter, dt);
+                } else {
+                    f.us = G2.us; f.ps = G2.ps;
+                }
+                f.psus = f.ps * f.us;
+                f.dtus = dt * f.us;
+                F4 = f;
+            }
+            // ---- Lagrange update of cell j = t - LAG_L ----
+            const int j = t - LAG_L;
+            if (j >= firstF) {
+                L1 = L2; L2 = L3;
+                L3 = lagrange(kGAD ? C0 : C1, F3, F4, dt, dx);
+                if (kE2) {
+                    d01 = d12; d12 = d23; d23 = lag_diff(L2, L3);
+                    s01 = s12; s12 = s23; s23 = L2.W + L3.W;
+                }
+            }
+            // ---- advection flux at face k = t - LAG_A ----
+            const int k = t - LAG_A;
+            if (k >= a0) {
+                A0 = A1;
+                A1 = kE2 ? advect2(F1, F2, F3, L1, L2, d01, d12, d23, s01, s12, s23, dx) : advect1(F3, L2, L3);
+            }
+            // ---- projection of cell mm = k - 1 ----
+            const int mm = k - 1;
+            if (mm >= a0) {
+                const Lag<T>& Lc = kE2 ? L1 : L2;
+                // src/kernels/euler_projection.cpp:36-46
+                T dXr = Lc.W * Lc.rho;
+                T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
+                T tmp_ra = div_dx(dXr * Lc.ua - (A1.ra - A0.ra), g);
+                T tmp_ro = div_dx(dXr * Lc.uo - (A1.ro - A0.ro), g);
+                T tmp_rE = div_dx(dXr * Lc.E - (A1.rE - A0.rE), g);
+                T ua = qdiv(tmp_ra, tmp_rho), uo = qdiv(tmp_ro, tmp_rho), E = qdiv(tmp_rE, tmp_rho);
+                const int64_t idx = base + (int64_t)mm * s;
+                out[0][idx] = tmp_rho;
+                out[axis == 0 ? 1 : 2][idx] = ua;
+                out[axis == 0 ? 2 : 1][idx] = uo;
+                out[3][idx] = E;
+                if (LAST) {
+                    // dt_CFL of the state after this pass, with c from this pass's EOS
+                    if (axis == 0) acc.add(ua, uo, Lc.c);
+                    else acc.add(uo, ua, Lc.c);
+                }
+            }
+        }
+    }
+
+    if constexpr (LAST) commit_cycle(A, acc, st, cd, blk, nblk);
 }
 
 // One domain: the whole grid works on it.

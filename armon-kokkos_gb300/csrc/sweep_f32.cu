@@ -1,6 +1,8 @@
 // sweep_f32.cu -- instantiation of the solver kernels for float storage and arithmetic.
-// Built with FMA contraction: the FP32 variant is compared with the FP64 oracle by tolerance
-// (dt and the conservation sums stay FP64).
+// Built without FMA contraction, like the FP64 units: every operation rounds on its own, so the
+// single-domain and the batched kernels (separately compiled) give the same bits, and a domain's
+// result does not depend on what it shares a launch with.  The FP32 variant is compared with the
+// FP64 oracle by tolerance (dt and the conservation sums stay FP64).
 #include "solver_kernels.cuh"
 
 namespace armon {

@@ -96,7 +96,7 @@ def test_batch_admission_removal_and_budget():
                 assert np.array_equal(A.real_cells(b.params[i], b.download(i, k)), ref[k]), k
 
 
-def test_batch_fp32_close_to_solo_fp32():
+def test_batch_fp32_identical_to_solo_fp32():
     specs = small_domains(5, seed=21)
     with A.Batch(precision=32) as b:
         ids = [b.add(s.params(), s.initial_state()) for s in specs]
@@ -105,9 +105,9 @@ def test_batch_fp32_close_to_solo_fp32():
             ps, _, ref = solo(spec, precision=32)
             pb, _ = b.state(i)
             assert pb.cycle == ps.cycle
-            for k in ("rho", "Emat"):
+            for k in FIELDS:
                 got = A.real_cells(b.params[i], b.download(i, k))
-                assert np.allclose(got, ref[k], rtol=1e-6, atol=0), k
+                assert np.array_equal(got, ref[k]), k
 
 
 def test_batch_segment_choice_does_not_change_results():

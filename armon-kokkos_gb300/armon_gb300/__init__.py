@@ -57,6 +57,28 @@ class BatchOpts(C.Structure):
                 ("seg_len", C.c_int32), ("memory_budget", C.c_int64)]
 
 
+class SodInterface(C.Structure):
+    """armon_sod_interface: a planar (shape 0) or circular (shape 1) Sod interface made on the device."""
+    _fields_ = [("shape", C.c_int32), ("reserved", C.c_int32), ("cx", C.c_double), ("cy", C.c_double),
+                ("nx", C.c_double), ("ny", C.c_double), ("offset", C.c_double), ("r2", C.c_double),
+                ("rho_high", C.c_double), ("p_high", C.c_double), ("rho_low", C.c_double), ("p_low", C.c_double)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_budget", C.c_int64), ("cycles_per_step", C.c_int32), ("block_lines", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
+
+
+class RequestInfo(C.Structure):
+    """armon_server_request."""
+    _fields_ = [("status", C.c_int32), ("precision", C.c_int32), ("cycle", C.c_int32), ("nx", C.c_int32),
+                ("ny", C.c_int32), ("pad", C.c_int32), ("time", C.c_double), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("bytes", C.c_int64)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
 class Range(C.Structure):
     _fields_ = [("start", C.c_int64), ("end", C.c_int64)]
 
@@ -117,6 +139,7 @@ def lib() -> C.CDLL:
     L.armon_batch_domain_bytes.argtypes = [P, C.c_int32]
     L.armon_batch_domain_bytes.restype = C.c_int64
     L.armon_batch_add.argtypes = [B, P, C.POINTER(C.c_void_p), C.POINTER(C.c_int32)]
+    L.armon_batch_add_sod.argtypes = [B, P, C.POINTER(SodInterface), C.POINTER(C.c_int32)]
     L.armon_batch_set_seg_len.argtypes = [B, C.c_int32, C.c_int32]
     L.armon_batch_enqueue_cycles.argtypes = [B, C.c_int32]
     L.armon_batch_run.argtypes = [B, C.c_int32, C.POINTER(C.c_int32)]
@@ -130,6 +153,22 @@ def lib() -> C.CDLL:
     L.armon_batch_bytes_in_use.restype = C.c_int64
     L.armon_batch_kernel_launches.argtypes = [B]
     L.armon_batch_kernel_launches.restype = C.c_int64
+    V = C.c_void_p
+    L.armon_server_opts_default.argtypes = [C.POINTER(ServerOpts)]
+    L.armon_server_opts_default.restype = None
+    L.armon_server_create.argtypes = [C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]
+    L.armon_server_destroy.argtypes = [V]
+    L.armon_server_destroy.restype = None
+    L.armon_server_submit.argtypes = [V, P, C.c_int32, C.POINTER(SodInterface), C.POINTER(C.c_int64)]
+    L.armon_server_step.argtypes = [V, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.armon_server_next_done.argtypes = [V, C.POINTER(C.c_int64)]
+    L.armon_server_request_info.argtypes = [V, C.c_int64, C.POINTER(RequestInfo)]
+    L.armon_server_download.argtypes = [V, C.c_int64, C.c_int, C.c_void_p]
+    L.armon_server_release.argtypes = [V, C.c_int64]
+    L.armon_server_bytes_in_use.argtypes = [V]
+    L.armon_server_bytes_in_use.restype = C.c_int64
+    L.armon_server_kernel_launches.argtypes = [V]
+    L.armon_server_kernel_launches.restype = C.c_int64
     L.dt_CFL.restype = C.c_double
     L.idx_size.restype = C.c_int
     L.is_uidx_signed.restype = C.c_bool
@@ -341,6 +380,14 @@ class Batch:
         self.params[i.value] = p
         return i.value
 
+    def add_sod(self, params: Params | Case, sod: SodInterface) -> int:
+        """Adds a domain initialised on the device with a Sod interface (armon_batch_add_sod)."""
+        p = make_params(params) if isinstance(params, Case) else params
+        i = C.c_int32()
+        check(lib().armon_batch_add_sod(self._h, C.byref(p), C.byref(sod), C.byref(i)))
+        self.params[i.value] = p
+        return i.value
+
     def set_seg_len(self, i: int, seg_len: int) -> None:
         check(lib().armon_batch_set_seg_len(self._h, i, seg_len))
 
@@ -386,3 +433,74 @@ class Batch:
 
 def domain_bytes(params: Params, precision: int = 64) -> int:
     return int(lib().armon_batch_domain_bytes(C.byref(params), precision))
+
+
+class Server:
+    """The request loop over batches (armon_server_* of include/armon_gb300.h)."""
+
+    def __init__(self, memory_budget: int = 150_000_000_000, cycles_per_step: int = 8, block_lines: int = 128):
+        L = lib()
+        o = ServerOpts()
+        L.armon_server_opts_default(C.byref(o))
+        o.memory_budget, o.cycles_per_step, o.block_lines = memory_budget, cycles_per_step, block_lines
+        h = C.c_void_p()
+        check(L.armon_server_create(C.byref(o), C.byref(h)))
+        self._h = h
+        self.params: dict[int, Params] = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().armon_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params: Params | Case, precision: int = 64, sod: SodInterface | None = None) -> int:
+        p = make_params(params) if isinstance(params, Case) else params
+        r = C.c_int64()
+        check(lib().armon_server_submit(self._h, C.byref(p), precision, C.byref(sod) if sod is not None else None,
+                                         C.byref(r)))
+        self.params[r.value] = p
+        return r.value
+
+    def step(self) -> tuple[int, int]:
+        """One round; returns (requests running, requests waiting)."""
+        a, b = C.c_int32(), C.c_int32()
+        check(lib().armon_server_step(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def next_done(self) -> int | None:
+        r = C.c_int64()
+        return r.value if lib().armon_server_next_done(self._h, C.byref(r)) == 1 else None
+
+    def info(self, req: int) -> RequestInfo:
+        i = RequestInfo()
+        check(lib().armon_server_request_info(self._h, req, C.byref(i)))
+        return i
+
+    def download(self, req: int, name: str) -> np.ndarray:
+        a = np.empty(self.params[req].nb_cells, dtype=np.float64)
+        check(lib().armon_server_download(self._h, req, ARRAYS.index(name), a.ctypes.data))
+        return a
+
+    def release(self, req: int) -> None:
+        check(lib().armon_server_release(self._h, req))
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(lib().armon_server_bytes_in_use(self._h))
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().armon_server_kernel_launches(self._h))
+

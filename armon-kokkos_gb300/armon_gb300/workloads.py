@@ -19,7 +19,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import Case, Params, make_params
+from . import Case, Params, SodInterface, make_params
 
 GAMMA = 1.4
 SIDES = (64, 128, 256, 512, 1024)
@@ -65,6 +65,21 @@ class DomainSpec:
         E = pr / ((GAMMA - 1) * rho)
         z = np.zeros_like(rho)
         return {"rho": rho.ravel(), "umat": z.ravel(), "vmat": z.ravel().copy(), "Emat": E.ravel()}
+
+    def sod_interface(self) -> SodInterface:
+        """The same initial state made on the device (armon_sod_interface): every operand and operation
+        of initial_state's tests, in the same order."""
+        s = SodInterface()
+        s.cx = s.cy = 0.5
+        if self.kind == "planar":
+            s.shape = 0
+            s.nx, s.ny = float(np.cos(self.angle)), float(np.sin(self.angle))
+            s.offset = self.pos - 0.5
+        else:
+            s.shape = 1
+            s.r2 = (self.pos / 2) ** 2
+        s.rho_high, s.p_high, s.rho_low, s.p_low = self.rho_l, self.p_l, self.rho_r, self.p_r
+        return s
 
     @property
     def cells(self) -> int:

@@ -25,6 +25,8 @@ CLI = os.path.join(HERE, "armon_gb300", "armon_gb300_2D")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--extended-lambda",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# extra nvcc flags for tuning builds (e.g. -DARMON_SWEEP_MIN_BLOCKS=3); rebuild with --clean
+EXTRA = os.environ.get("ARMON_NVCC_FLAGS", "").split()
 
 # (source, extra flags)
 UNITS = [
@@ -35,6 +37,7 @@ UNITS = [
     ("batch.cu", ["--fmad=false"]),
     ("selftest.cu", ["--fmad=false"]),
     ("params.cpp", []),
+    ("server.cpp", []),
     ("armon_2D.cpp", []),
 ]
 CLI_SRC = "main_2D.cpp"
@@ -67,7 +70,7 @@ def _compile(src: str, flags: list[str], verbose: bool) -> str:
     if _newer(obj, [path] + _headers() + [os.path.abspath(__file__)]):
         return obj
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
-    cmd = [nvcc()] + ARCH + COMMON + flags + lang + ["-c", path, "-o", obj]
+    cmd = [nvcc()] + ARCH + COMMON + EXTRA + flags + lang + ["-c", path, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

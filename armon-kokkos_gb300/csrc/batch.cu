@@ -277,7 +277,14 @@ void armon_batch_destroy(armon_batch* b)
     delete b;
 }
 
-int armon_batch_add(armon_batch* b, const armon_params* p, const double* const init[4], int32_t* id)
+}  // extern "C"
+
+namespace {
+
+// armon_batch_add / armon_batch_add_sod: the initial state from init_test, then from the host
+// arrays `init` or the interface `sod` when given.
+int add_domain(armon_batch* b, const armon_params* p, const double* const init[4], const armon_sod_interface* sod,
+               int32_t* id)
 {
     *id = -1;
     int rc = check_supported(p);
@@ -332,7 +339,18 @@ int armon_batch_add(armon_batch* b, const armon_params* p, const double* const i
                 nullptr, nullptr};
     CUDA_TRY(launch_init(a, p->nb_cells, ip, b->fp32, b->stream));
     b->launches++;
-    if (init) {
+    if (sod) {
+        SodInit si{};
+        si.row_length = p->row_length; si.nb_ghosts = p->nb_ghosts; si.nx = p->nx; si.ny = p->ny;
+        si.sx = p->domain_size[0]; si.sy = p->domain_size[1]; si.ox = p->domain_origin[0]; si.oy = p->domain_origin[1];
+        si.shape = sod->shape;
+        si.cx = sod->cx; si.cy = sod->cy; si.nxv = sod->nx; si.nyv = sod->ny; si.offset = sod->offset; si.r2 = sod->r2;
+        const double gm1 = 1.4 - 1.0;
+        si.rho_high = sod->rho_high; si.E_high = sod->p_high / (gm1 * sod->rho_high);
+        si.rho_low = sod->rho_low; si.E_low = sod->p_low / (gm1 * sod->rho_low);
+        CUDA_TRY(launch_init_sod(si, p->nb_cells, dd.arr[0], dd.arr[1], dd.arr[2], dd.arr[3], b->fp32, b->stream));
+        b->launches++;
+    } else if (init) {
         // rho umat vmat Emat of set 0
         for (int k = 0; k < 4; k++) {
             if (!init[k]) continue;
@@ -365,6 +383,22 @@ int armon_batch_add(armon_batch* b, const armon_params* p, const double* const i
     b->dirty = true;
     *id = slot;
     return ARMON_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int armon_batch_add(armon_batch* b, const armon_params* p, const double* const init[4], int32_t* id)
+{
+    return add_domain(b, p, init, nullptr, id);
+}
+
+int armon_batch_add_sod(armon_batch* b, const armon_params* p, const armon_sod_interface* sod, int32_t* id)
+{
+    if (!sod) { *id = -1; set_error("no interface given"); return ARMON_ERR_PARAMS; }
+    if (sod->shape != 0 && sod->shape != 1) { *id = -1; set_error("interface shape must be 0 or 1"); return ARMON_ERR_PARAMS; }
+    return add_domain(b, p, nullptr, sod, id);
 }
 
 int armon_batch_set_seg_len(armon_batch* b, int32_t id, int32_t seg_len)

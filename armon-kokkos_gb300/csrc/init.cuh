@@ -89,4 +89,30 @@ __device__ __forceinline__ void init_cell(const InitArgs& a, int64_t i, T* x, T*
     if (pstar) pstar[i] = 0;
 }
 
+// A Sod-type interface state over all cells (armon_sod_interface of include/armon_gb300.h): cell
+// centres as init_cell computes them, then the planar or circular test, in FP64 for every storage
+// type; u = v = 0.  E_high / E_low are p / ((1.4 - 1) rho) of each state.
+struct SodInit {
+    int64_t row_length, nb_ghosts, nx, ny;
+    double sx, sy, ox, oy;
+    int32_t shape, pad;
+    double cx, cy, nxv, nyv, offset, r2;
+    double rho_high, E_high, rho_low, E_low;
+};
+
+template <class T>
+__device__ __forceinline__ void init_sod_cell(const SodInit& a, int64_t i, T* rho, T* umat, T* vmat, T* Emat)
+{
+    const int64_t ix = (i % a.row_length) - a.nb_ghosts;
+    const int64_t iy = (i / a.row_length) - a.nb_ghosts;
+    const double x = double(ix) / double(a.nx) * a.sx + a.ox + a.sx / double(2 * a.nx);
+    const double y = double(iy) / double(a.ny) * a.sy + a.oy + a.sy / double(2 * a.ny);
+    const double dx = x - a.cx, dy = y - a.cy;
+    const bool high = a.shape == 0 ? dx * a.nxv + dy * a.nyv <= a.offset : dx * dx + dy * dy <= a.r2;
+    rho[i] = T(high ? a.rho_high : a.rho_low);
+    Emat[i] = T(high ? a.E_high : a.E_low);
+    umat[i] = T(0);
+    vmat[i] = T(0);
+}
+
 }  // namespace armon

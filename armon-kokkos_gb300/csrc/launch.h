@@ -1,6 +1,6 @@
 // launch.h -- host-side launchers of the solver kernels, one overload per storage type.
-// sweep_f64.cu (built with --fmad=false: bit-exact FP64) and sweep_f32.cu (FP32 with FMA
-// contraction) define them; solver.cu drives them.
+// sweep_f64.cu and sweep_f32.cu (both built with --fmad=false) define them; solver.cu and
+// batch.cu drive them.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -31,6 +31,18 @@ cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p
 inline cudaError_t launch_init(const InitArgs& a, int64_t ncells, const InitPtrs& p, bool fp32, cudaStream_t st)
 {
     return fp32 ? launch_init_f32(a, ncells, p, st) : launch_init_f64(a, ncells, p, st);
+}
+
+// The Sod-interface state (init.cuh: SodInit) over all ncells cells.
+cudaError_t launch_init_sod_f64(const SodInit& a, int64_t ncells, void* rho, void* umat, void* vmat, void* Emat,
+                                cudaStream_t st);
+cudaError_t launch_init_sod_f32(const SodInit& a, int64_t ncells, void* rho, void* umat, void* vmat, void* Emat,
+                                cudaStream_t st);
+inline cudaError_t launch_init_sod(const SodInit& a, int64_t ncells, void* rho, void* umat, void* vmat, void* Emat,
+                                   bool fp32, cudaStream_t st)
+{
+    return fp32 ? launch_init_sod_f32(a, ncells, rho, umat, vmat, Emat, st)
+                : launch_init_sod_f64(a, ncells, rho, umat, vmat, Emat, st);
 }
 
 // EOS of the real cells + dt_CFL of that state + reset of the loop state (the start of time_loop,

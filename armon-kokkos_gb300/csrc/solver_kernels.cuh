@@ -15,6 +15,13 @@ __global__ void init_kernel(InitArgs a, int64_t ncells, InitPtrs p)
                      (T*)p.pmat, (T*)p.cmat, (T*)p.gmat, (T*)p.ustar, (T*)p.pstar);
 }
 
+template <class T>
+__global__ void init_sod_kernel(SodInit a, int64_t ncells, T* rho, T* umat, T* vmat, T* Emat)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncells; i += (int64_t)gridDim.x * blockDim.x)
+        init_sod_cell<T>(a, i, rho, umat, vmat, Emat);
+}
+
 // Shared tail of the dt reductions: block max of (ax, ay), partial per block, and the last block
 // to finish returns true with the grid maxima in (*gx, *gy) (thread 0 only).
 __device__ inline bool grid_dt_maxima(DtAcc acc, double* partials, uint32_t* counter, double* gx, double* gy)

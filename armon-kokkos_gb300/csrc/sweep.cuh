@@ -43,6 +43,11 @@
 #define ARMON_SOFT_FP64 1
 #endif
 
+// Blocks of 128 threads the compiler must fit on one SM (it caps registers accordingly).
+#ifndef ARMON_SWEEP_MIN_BLOCKS
+#define ARMON_SWEEP_MIN_BLOCKS 2
+#endif
+
 namespace armon {
 
 template <class T>
@@ -496,7 +501,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
 
 // One domain: the whole grid works on it.
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(128, ARMON_SWEEP_MIN_BLOCKS) sweep_kernel(const SweepArgs<T> A)
 {
     sweep_domain<T, SCHEME, PROJ, LAST>(A, blockIdx.x, gridDim.x, A.pass);
 }
@@ -505,7 +510,7 @@ __global__ void __launch_bounds__(128) sweep_kernel(const SweepArgs<T> A)
 // grid (enough for its larger axis); each domain keeps its own step state, so dt, time and cycle
 // advance per domain and a finished domain's blocks return at once.
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
+__global__ void __launch_bounds__(128, ARMON_SWEEP_MIN_BLOCKS) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
                                                           const int* __restrict__ offsets, int ndom, int pass)
 {
     const int b = blockIdx.x;

@@ -28,6 +28,16 @@ cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p
     return cudaGetLastError();
 }
 
+cudaError_t launch_init_sod_f32(const SodInit& a, int64_t ncells, void* rho, void* umat, void* vmat, void* Emat,
+                                cudaStream_t st)
+{
+    int64_t blocks = (ncells + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (blocks < 1) blocks = 1;
+    init_sod_kernel<float><<<(int)blocks, 256, 0, st>>>(a, ncells, (float*)rho, (float*)umat, (float*)vmat, (float*)Emat);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_begin_f32(const BeginArgs& a, int grid, cudaStream_t st)
 {
     begin_kernel<float><<<grid, 256, 0, st>>>(a);

@@ -26,6 +26,16 @@ cudaError_t launch_init_f64(const InitArgs& a, int64_t ncells, const InitPtrs& p
     return cudaGetLastError();
 }
 
+cudaError_t launch_init_sod_f64(const SodInit& a, int64_t ncells, void* rho, void* umat, void* vmat, void* Emat,
+                                cudaStream_t st)
+{
+    int64_t blocks = (ncells + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (blocks < 1) blocks = 1;
+    init_sod_kernel<double><<<(int)blocks, 256, 0, st>>>(a, ncells, (double*)rho, (double*)umat, (double*)vmat, (double*)Emat);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_begin_f64(const BeginArgs& a, int grid, cudaStream_t st)
 {
     begin_kernel<double><<<grid, 256, 0, st>>>(a);

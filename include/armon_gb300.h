@@ -165,6 +165,26 @@ int64_t armon_batch_domain_bytes(const armon_params* p, int32_t precision);
  * scheme, projection and axis splitting.  *id receives the domain's handle. */
 int armon_batch_add(armon_batch* b, const armon_params* p, const double* const init[4], int32_t* id);
 
+/* A Sod-type initial state made on the device (no counterpart in the reference, whose tests have
+ * axis-aligned or fixed-radius interfaces).  Cell centres follow init_test
+ * (src/kernels/init_test.cpp:65-93): x = ix / nx * sx + ox + sx / (2 nx), the same for y.  The high
+ * state (rho_high, p_high) holds where
+ *   shape 0 (planar):   (x - cx) * nx + (y - cy) * ny <= offset
+ *   shape 1 (circular): (x - cx) * (x - cx) + (y - cy) * (y - cy) <= r2
+ * and the low state elsewhere, with u = v = 0 and E = p / ((1.4 - 1) rho), over all nb_cells
+ * cells (ghosts included); every operation is one IEEE-rounded FP64 operation in that order. */
+typedef struct armon_sod_interface {
+    int32_t shape;
+    int32_t reserved;
+    double cx, cy;
+    double nx, ny, offset;    /* planar */
+    double r2;                /* circular */
+    double rho_high, p_high, rho_low, p_low;
+} armon_sod_interface;
+
+/* armon_batch_add with the initial state of `sod` instead of host arrays. */
+int armon_batch_add_sod(armon_batch* b, const armon_params* p, const armon_sod_interface* sod, int32_t* id);
+
 /* Cells per thread along the sweep axis for one domain (0 = automatic); takes effect at the next
  * launch.  Results do not depend on it. */
 int armon_batch_set_seg_len(armon_batch* b, int32_t id, int32_t seg_len);
@@ -193,6 +213,63 @@ int armon_batch_remove(armon_batch* b, int32_t id);
 int32_t armon_batch_size(armon_batch* b);                /* domains held */
 int64_t armon_batch_bytes_in_use(armon_batch* b);
 int64_t armon_batch_kernel_launches(armon_batch* b);
+
+/* ---- serving: a request loop over batches (no counterpart in the reference) ----
+ * Solves are submitted as requests and wait in a first-come-first-served queue.  Each round
+ * admits waiting requests while their state fits in the memory budget, then advances every
+ * admitted solve by a few cycles: solves of one precision and scheme share a batch (one fused
+ * launch per pass for all of them), different batches run on their own streams and overlap on the
+ * device.  A solve's state stays on the device from admission until the caller releases it;
+ * finished solves leave the launch tables at once, and released memory admits the next requests.
+ * A request gives the same result as the same solve run alone. */
+typedef struct armon_server armon_server;
+
+typedef struct armon_server_opts {
+    int64_t memory_budget;     /* device bytes of solve state held at once (default 150e9) */
+    int32_t cycles_per_step;   /* cycles of every running solve per round (default 8) */
+    int32_t block_lines;       /* as armon_batch_opts (default 128) */
+    int32_t reserved[4];
+} armon_server_opts;
+
+enum { ARMON_REQ_QUEUED = 0, ARMON_REQ_RUNNING = 1, ARMON_REQ_DONE = 2, ARMON_REQ_FAILED = 3 };
+
+typedef struct armon_server_request {
+    int32_t status;            /* ARMON_REQ_* (FAILED: the solve stopped on an invalid dt) */
+    int32_t precision;
+    int32_t cycle;             /* cycles done when it finished */
+    int32_t nx, ny;
+    int32_t pad;
+    double time;               /* simulated time reached */
+    double t_submit, t_admit, t_done;   /* seconds since the server was created (-1: not yet) */
+    int64_t bytes;             /* device bytes of its state */
+} armon_server_request;
+
+void armon_server_opts_default(armon_server_opts* o);
+int armon_server_create(const armon_server_opts* opts, armon_server** out);
+void armon_server_destroy(armon_server* s);
+
+/* Queues a solve (p as for armon_batch_add; max_time and max_cycles end it) in precision 64 or 32,
+ * initialised from `sod`, or by init_test when it is NULL.  *req receives its id. */
+int armon_server_submit(armon_server* s, const armon_params* p, int32_t precision, const armon_sod_interface* sod,
+                        int64_t* req);
+
+/* One round: admission, cycles_per_step cycles of every running solve, retirement of the solves
+ * that finished.  *in_flight / *queued (may be NULL) receive the running / waiting requests. */
+int armon_server_step(armon_server* s, int32_t* in_flight, int32_t* queued);
+
+/* Pops the next finished (done or failed) request not yet reported: returns 1 and sets *req, or 0. */
+int armon_server_next_done(armon_server* s, int64_t* req);
+
+int armon_server_request_info(armon_server* s, int64_t req, armon_server_request* info);
+
+/* Downloads one array of a finished request (which as armon_batch_download). */
+int armon_server_download(armon_server* s, int64_t req, int which, double* host);
+
+/* Frees a finished request's device state. */
+int armon_server_release(armon_server* s, int64_t req);
+
+int64_t armon_server_bytes_in_use(armon_server* s);
+int64_t armon_server_kernel_launches(armon_server* s);
 
 /* One full solve with host buffers, the reference-facing end-to-end call: uploads rho, umat,
  * vmat, Emat (and the rest of the initial state made by init_test on the device), runs the time

@@ -54,7 +54,7 @@ class SolverOpts(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("block_lines", C.c_int32),
-                ("seg_len", C.c_int32), ("memory_budget", C.c_int64)]
+                ("seg_len", C.c_int32), ("memory_budget", C.c_int64), ("waves", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SodInterface(C.Structure):
@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
     L.armon_batch_domain_done.argtypes = [B, C.c_int32]
     L.armon_batch_download.argtypes = [B, C.c_int32, C.c_int, C.c_void_p]
     L.armon_batch_remove.argtypes = [B, C.c_int32]
+    L.armon_batch_schedule.argtypes = [B, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.armon_batch_size.argtypes = [B]
     L.armon_batch_bytes_in_use.argtypes = [B]
     L.armon_batch_bytes_in_use.restype = C.c_int64
@@ -335,12 +336,12 @@ class Batch:
     """Many independent domains advanced together (armon_batch_* of include/armon_gb300.h)."""
 
     def __init__(self, precision: int = 64, stream: int | None = None, cycles_per_graph: int = 8,
-                 block_lines: int = 128, seg_len: int = 0, memory_budget: int = 0):
+                 block_lines: int = 128, seg_len: int = 0, memory_budget: int = 0, waves: int = 0):
         L = lib()
         o = BatchOpts()
         L.armon_batch_opts_default(C.byref(o))
         o.precision, o.cycles_per_graph, o.block_lines = precision, cycles_per_graph, block_lines
-        o.seg_len, o.memory_budget = seg_len, memory_budget
+        o.seg_len, o.memory_budget, o.waves = seg_len, memory_budget, waves
         h = C.c_void_p()
         check(L.armon_batch_create(C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
         self._h = h
@@ -421,6 +422,12 @@ class Batch:
     def remove(self, i: int) -> None:
         check(lib().armon_batch_remove(self._h, i))
         self.params.pop(i, None)
+
+    def schedule(self) -> tuple[int, int]:
+        """(block waves per launch in use, blocks of the current launch table)."""
+        w, n = C.c_int32(), C.c_int32()
+        check(lib().armon_batch_schedule(self._h, C.byref(w), C.byref(n)))
+        return w.value, n.value
 
     @property
     def bytes_in_use(self) -> int:

@@ -8,7 +8,9 @@
 // domains join or finish; cycles are captured in a CUDA graph per table.  The host reads all
 // step states back with one copy per graph batch.
 #include <algorithm>
+#include <array>
 #include <cstring>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -22,6 +24,21 @@ using namespace armon;
 namespace {
 
 constexpr int kMaxDomains = 8192;
+
+// Candidates of the autotuned schedule (block waves per launch), and the least running cells for
+// which tuning is worth a graph batch per candidate.
+constexpr int kWaves[] = {2, 4, 8, 16, 64};
+constexpr int kNumWaves = sizeof(kWaves) / sizeof(kWaves[0]);
+constexpr int64_t kTuneMinCells = 1 << 21;
+
+struct Tuner {
+    int phase = 0;              // 0 never tuned, 1 timing candidates, 2 tuned
+    int cand = 0;
+    bool launched = false;      // the current candidate's graph batch is on the stream
+    double work = 0;            // its cell-updates
+    double rate[kNumWaves] = {};
+    int64_t tuned_cells = 0;    // running cells when tuning started
+};
 
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
@@ -64,6 +81,10 @@ struct armon_batch {
     int* d_offsets = nullptr;
     std::vector<int> table;
     int total_blocks = 0;
+    int blocks_per_sm = 0;        // of the batch kernel (0: not yet known)
+    int waves = 8;                // block waves per launch the schedule aims for
+    Tuner tune;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool dirty = true;
     cudaGraphExec_t graph = nullptr;
     int64_t bytes = 0;
@@ -91,17 +112,76 @@ DomainBuffers<T> buffers(const Dom& d)
     return DomainBuffers<T>{{{a[0], a[1], a[2], a[3]}, {a[4], a[5], a[6], a[7]}}, a[8], a[9], a[10]};
 }
 
+// Segment lengths of the running domains, both axes, for one launch over all of them.  Each axis
+// starts as whole lines (one segment per line); then the longest segments are split while they
+// are longer than 1 / waves of the average load of a resident block slot, and never below 16
+// cells.  A launch lasts at least as long as its longest block and at least as long as its total
+// work over the slots; a block's work is seg_len + 1.2 * halo thread-steps (the halo is recomputed
+// per segment).  Few waves keep the recomputation low, more waves shorten the tail of the launch
+// where the last blocks run alone; the batch autotunes the number.
+std::vector<std::array<int, 2>> schedule_segments(const armon_batch* b)
+{
+    const int block = b->o.block_lines;
+    const double slots = double(b->sm_count) * std::max(1, b->blocks_per_sm);
+    const size_t nd = b->table.size();
+    std::vector<std::array<int, 2>> seg(nd, {0, 0});
+    struct Item {
+        int n, nlines, nseg;
+        double halo, len, blocks;
+    };
+    for (int axis = 0; axis < 2; axis++) {
+        std::vector<Item> it(nd);
+        std::priority_queue<std::pair<double, int>> heap;   // (block length, item)
+        double total = 0;
+        for (size_t k = 0; k < nd; k++) {
+            const armon_params& p = b->doms[b->table[k]].p;
+            Item& x = it[k];
+            x.n = axis == 0 ? p.nx : p.ny;
+            x.nlines = axis == 0 ? p.ny : p.nx;
+            x.nseg = 1;
+            x.halo = 1.2 * stencil_reach(&p);
+            const AxisTiling t = axis_tiling(x.n, x.nlines, block, x.n);
+            x.len = t.seg_len + x.halo;
+            x.blocks = t.blocks;
+            total += x.blocks * x.len;
+            heap.push({x.len, (int)k});
+        }
+        while (!heap.empty()) {
+            const int k = heap.top().second;
+            Item& x = it[k];
+            if (x.len <= total / (slots * b->waves)) break;
+            const int nseg = std::max(x.nseg + 1, x.nseg * 5 / 4);
+            const int sl = (x.n + nseg - 1) / nseg;
+            if (sl < 16) break;                   // the longest block cannot get shorter
+            heap.pop();
+            const AxisTiling t = axis_tiling(x.n, x.nlines, block, sl);
+            total -= x.blocks * x.len;
+            x.nseg = t.nseg;
+            x.len = t.seg_len + x.halo;
+            x.blocks = t.blocks;
+            total += x.blocks * x.len;
+            heap.push({x.len, k});
+        }
+        for (size_t k = 0; k < nd; k++) seg[k][axis] = (it[k].n + it[k].nseg - 1) / it[k].nseg;
+    }
+    return seg;
+}
+
 template <class T>
 int rebuild_t(armon_batch* b)
 {
     b->table.clear();
     for (int i = 0; i < (int)b->doms.size(); i++)
         if (b->doms[i].used && !b->doms[i].done) b->table.push_back(i);
+    if (b->blocks_per_sm == 0 && !b->table.empty())
+        b->blocks_per_sm = sweep_batch_blocks_per_sm(b->fp32, b->scheme, b->proj, b->o.block_lines);
+    const std::vector<std::array<int, 2>> sched = schedule_segments(b);
     std::vector<SweepArgs<T>> args(b->table.size());
     std::vector<int> offsets(b->table.size() + 1, 0);
     for (size_t k = 0; k < b->table.size(); k++) {
         Dom& d = b->doms[b->table[k]];
-        int forced = d.seg_len > 0 ? d.seg_len : b->o.seg_len;
+        const int fixed = d.seg_len > 0 ? d.seg_len : b->o.seg_len;
+        const int forced[2] = {fixed > 0 ? fixed : sched[k][0], fixed > 0 ? fixed : sched[k][1]};
         int nb = make_sweep_args<T>(d.p, b->npass, b->o.block_lines, b->sm_count, forced, buffers<T>(d),
                                     b->d_states + b->table[k], d.partials, 1, args[k]);
         if (nb > d.npartials) { set_error("domain needs more partial slots than allotted"); return ARMON_ERR_STATE; }
@@ -125,6 +205,56 @@ int rebuild_t(armon_batch* b)
 
 int rebuild(armon_batch* b) { return b->fp32 ? rebuild_t<float>(b) : rebuild_t<double>(b); }
 
+int64_t table_cells(const armon_batch* b)
+{
+    int64_t c = 0;
+    for (int i : b->table) c += (int64_t)b->doms[i].p.nx * b->doms[i].p.ny;
+    return c;
+}
+
+bool schedule_fixed(const armon_batch* b) { return b->o.waves > 0 || b->o.seg_len > 0; }
+
+// Online autotuning of the schedule: each candidate number of waves is timed with CUDA events over
+// one graph batch of real cycles (results do not depend on the segments, so nothing is wasted);
+// the fastest is kept until the running cells change by a factor of two.
+int tune_collect(armon_batch* b)
+{
+    Tuner& t = b->tune;
+    if (t.phase != 1 || !t.launched) return ARMON_OK;
+    CUDA_TRY(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    t.rate[t.cand] = ms > 0 ? t.work / ms : 0;
+    t.launched = false;
+    if (++t.cand < kNumWaves) {
+        b->waves = kWaves[t.cand];
+    } else {
+        int best = 0;
+        for (int k = 1; k < kNumWaves; k++)
+            if (t.rate[k] > t.rate[best]) best = k;
+        b->waves = kWaves[best];
+        t.phase = 2;
+    }
+    b->dirty = true;
+    return ARMON_OK;
+}
+
+bool tune_start(armon_batch* b)
+{
+    Tuner& t = b->tune;
+    if (schedule_fixed(b) || t.phase == 1) return false;
+    const int64_t cells = table_cells(b);
+    if (cells < kTuneMinCells) return false;
+    if (t.phase == 2 && cells * 2 > t.tuned_cells && cells < t.tuned_cells * 2) return false;
+    t.phase = 1;
+    t.cand = 0;
+    t.launched = false;
+    t.tuned_cells = cells;
+    b->waves = kWaves[0];
+    b->dirty = true;
+    return true;
+}
+
 int enqueue_direct(armon_batch* b, int n)
 {
     const int nd = (int)b->table.size();
@@ -145,8 +275,14 @@ int enqueue_direct(armon_batch* b, int n)
 
 int enqueue(armon_batch* b, int n)
 {
+    int rc = tune_collect(b);
+    if (rc != ARMON_OK) return rc;
     if (b->dirty) {
-        int rc = rebuild(b);
+        rc = rebuild(b);
+        if (rc != ARMON_OK) return rc;
+    }
+    if (tune_start(b)) {
+        rc = rebuild(b);
         if (rc != ARMON_OK) return rc;
     }
     if (b->table.empty() || n <= 0) return ARMON_OK;
@@ -166,7 +302,14 @@ int enqueue(armon_batch* b, int n)
             if (e != cudaSuccess) { b->graph = nullptr; return cuda_fail(e, "cudaGraphInstantiate"); }
         }
         while (n >= gc) {
+            const bool timed = b->tune.phase == 1 && !b->tune.launched;
+            if (timed) CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
             CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
+            if (timed) {
+                CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
+                b->tune.launched = true;
+                b->tune.work = double(table_cells(b)) * gc;
+            }
             b->launches += (int64_t)gc * b->npass;
             n -= gc;
         }
@@ -203,6 +346,7 @@ void armon_batch_opts_default(armon_batch_opts* o)
     o->precision = 64;
     o->cycles_per_graph = 8;
     o->block_lines = 128;
+    o->waves = 0;
 }
 
 int64_t armon_batch_domain_bytes(const armon_params* p, int32_t precision)
@@ -225,6 +369,7 @@ int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch**
     }
     b->fp32 = b->o.precision == 32;
     b->elem = b->fp32 ? 4 : 8;
+    if (b->o.waves > 0) b->waves = b->o.waves;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
@@ -247,6 +392,8 @@ int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch**
             e = cudaMemPoolSetAttribute(b->pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
     }
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(StepState) * kMaxDomains);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_states, sizeof(StepState) * kMaxDomains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_args, sizeof(SweepArgs<double>) * kMaxDomains);
@@ -273,6 +420,8 @@ void armon_batch_destroy(armon_batch* b)
     if (b->h_states) cudaFreeHost(b->h_states);
     if (b->d_args) cudaFree(b->d_args);
     if (b->d_offsets) cudaFree(b->d_offsets);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -498,6 +647,13 @@ int armon_batch_remove(armon_batch* b, int32_t id)
     b->bytes -= d.bytes;
     d = Dom();
     b->dirty = true;
+    return ARMON_OK;
+}
+
+int armon_batch_schedule(armon_batch* b, int32_t* waves, int32_t* blocks)
+{
+    if (waves) *waves = b->o.waves > 0 ? b->o.waves : b->waves;
+    if (blocks) *blocks = b->total_blocks;
     return ARMON_OK;
 }
 

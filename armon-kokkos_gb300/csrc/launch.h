@@ -22,6 +22,14 @@ cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets
 cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks, int pass,
                                int scheme, int proj, bool last, int block, cudaStream_t st);
 
+// Blocks of the batch kernel (last pass of a cycle) resident on one SM.
+int sweep_batch_blocks_per_sm_f64(int scheme, int proj, int block);
+int sweep_batch_blocks_per_sm_f32(int scheme, int proj, int block);
+inline int sweep_batch_blocks_per_sm(bool fp32, int scheme, int proj, int block)
+{
+    return fp32 ? sweep_batch_blocks_per_sm_f32(scheme, proj, block) : sweep_batch_blocks_per_sm_f64(scheme, proj, block);
+}
+
 // init_test over all nb_cells cells (src/kernels/init_test.cpp:51-104).
 struct InitPtrs {
     void *x, *y, *rho, *Emat, *umat, *vmat, *mask, *pmat, *cmat, *gmat, *ustar, *pstar;

@@ -66,7 +66,8 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
     T* const* arr = reinterpret_cast<T* const*>(s->arr);
     // set 0: rho umat vmat Emat; set 1: the four work arrays (free in the fused path)
     DomainBuffers<T> b{{{arr[2], arr[3], arr[4], arr[5]}, {arr[11], arr[12], arr[13], arr[14]}}, arr[6], arr[7], arr[8]};
-    s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, s->o.seg_len, b, s->d_state, s->d_partials,
+    const int forced[2] = {s->o.seg_len, s->o.seg_len};
+    s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, forced, b, s->d_state, s->d_partials,
                                  s->o.materialize_eos, a);
 }
 

@@ -26,29 +26,51 @@ inline bool is_pow2(double x)
     return x > 0 && m == 0.5;
 }
 
-// Segments along the axis: minimise (most blocks on one SM) x (cells a thread walks, halo
-// included) over the segment count, with segments of at least 16 cells.
-inline void choose_segments(int n, int nlines, int block, int halo, int sms, int forced, int* seg_len, int* nseg,
-                            int* nlb)
+// Lines per block for an axis of nlines lines: the whole block when there are that many lines,
+// else the lines rounded up to a multiple of 32 that divides the block, which then holds
+// block / lpb segments of the same lines.
+inline int lines_per_block(int nlines, int block)
 {
-    *nlb = std::max(1, (nlines + block - 1) / block);
-    if (forced > 0) {
-        *seg_len = std::min(forced, n);
-        *nseg = (n + *seg_len - 1) / *seg_len;
-        return;
-    }
+    int l = std::max(32, (nlines + 31) / 32 * 32);
+    if (l >= block) return block;
+    while (block % l != 0) l += 32;
+    return l;
+}
+
+// The blocks of one axis for a given segment length.
+struct AxisTiling {
+    int seg_len, nseg, nlb, lpb, spb, blocks;
+};
+
+inline AxisTiling axis_tiling(int n, int nlines, int block, int seg_len)
+{
+    AxisTiling t;
+    t.lpb = lines_per_block(nlines, block);
+    t.spb = block / t.lpb;
+    t.nlb = std::max(1, (nlines + t.lpb - 1) / t.lpb);
+    t.seg_len = std::max(1, std::min(seg_len, n));
+    t.nseg = (n + t.seg_len - 1) / t.seg_len;
+    t.blocks = t.nlb * ((t.nseg + t.spb - 1) / t.spb);
+    return t;
+}
+
+// Segments along the axis of one domain that has the GPU to itself: minimise (most blocks on one
+// SM) x (cells a thread walks, halo included) over the segment count, with segments of at least
+// 16 cells.  forced > 0 imposes the segment length.
+inline AxisTiling choose_segments(int n, int nlines, int block, int halo, int sms, int forced)
+{
+    if (forced > 0) return axis_tiling(n, nlines, block, forced);
     double best = 1e300;
     int best_seg = n;
     for (int ns = 1; ns <= std::max(1, n / 16); ns++) {
         int sl = (n + ns - 1) / ns;
         if ((int64_t)sl * (ns - 1) >= n) continue;
-        int64_t blocks = (int64_t)(*nlb) * ns;
-        double per_sm = std::ceil(double(blocks) / sms);
+        AxisTiling t = axis_tiling(n, nlines, block, sl);
+        double per_sm = std::ceil(double(t.blocks) / sms);
         double cost = per_sm * (sl + 1.2 * halo);
         if (cost < best - 1e-9) { best = cost; best_seg = sl; }
     }
-    *seg_len = best_seg;
-    *nseg = (n + best_seg - 1) / best_seg;
+    return axis_tiling(n, nlines, block, best_seg);
 }
 
 inline int check_supported(const armon_params* p)
@@ -94,10 +116,10 @@ struct DomainBuffers {
 };
 
 // Fills the argument block of the fused pass for one domain; returns the blocks it needs (the
-// larger of its two axes).
+// larger of its two axes).  forced_seg[axis] > 0 imposes that axis's segment length.
 template <class T>
-int make_sweep_args(const armon_params& p, int npass, int block, int sms, int forced_seg, const DomainBuffers<T>& b,
-                    StepState* state, double* partials, int write_eos, SweepArgs<T>& a)
+int make_sweep_args(const armon_params& p, int npass, int block, int sms, const int forced_seg[2],
+                    const DomainBuffers<T>& b, StepState* state, double* partials, int write_eos, SweepArgs<T>& a)
 {
     const int halo = stencil_reach(&p);
     for (int axis = 0; axis < 2; axis++) {
@@ -106,8 +128,13 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, int fo
         g.nlines = axis == 0 ? p.ny : p.nx;
         g.s = axis == 0 ? 1 : p.row_length;
         g.lstride = axis == 0 ? p.row_length : 1;
-        choose_segments(g.n, g.nlines, block, halo, sms, forced_seg, &g.seg_len, &g.nseg, &g.nlb);
-        g.blocks = g.nlb * g.nseg;
+        const AxisTiling t = choose_segments(g.n, g.nlines, block, halo, sms, forced_seg[axis]);
+        g.seg_len = t.seg_len;
+        g.nseg = t.nseg;
+        g.nlb = t.nlb;
+        g.lpb = t.lpb;
+        g.spb = t.spb;
+        g.blocks = t.blocks;
         // BC sign factors: X pass low = Left, high = Right; Y pass low = Bottom (y = -1), high = Top.
         double lo_u, lo_v, hi_u, hi_v;
         armon_boundary_factors(p.test, axis == 0 ? ARMON_LEFT : ARMON_BOTTOM, &lo_u, &lo_v);

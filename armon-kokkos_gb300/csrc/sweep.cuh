@@ -56,8 +56,8 @@ struct AxisGeom {
     int32_t nlines;     // lines (rows for X, columns for Y)
     int32_t seg_len;    // real cells per thread
     int32_t nseg;       // segments per line
-    int32_t nlb;        // blocks of lines (ceil(nlines / blockDim.x))
-    int32_t blocks;     // nlb * nseg
+    int32_t nlb;        // blocks of lines (ceil(nlines / lpb))
+    int32_t blocks;     // nlb * ceil(nseg / spb)
     int64_t s;          // stride along the axis
     int64_t lstride;    // stride between lines
     T fa_lo, fo_lo, fa_hi, fo_hi;   // sign factors of the axis / other velocity, low / high side
@@ -66,6 +66,8 @@ struct AxisGeom {
     uint32_t fneg;      // bit k set: factor k (fa_lo, fo_lo, fa_hi, fo_hi) is -1
     int32_t f_unit;     // every factor is +1 or -1: apply them as sign flips
     int32_t dx_log2;    // dx == 2^dx_log2 when dx_pow2
+    int32_t lpb;        // lines per block: a multiple of 32 dividing blockDim.x
+    int32_t spb;        // segments per block: blockDim.x / lpb (narrow domains fill a block with segments)
 };
 
 template <class T>
@@ -368,10 +370,14 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
     acc.init();
     const T gamma_m1 = A.gamma - 1;
 
+    // block blk = (line block lb, segment block sb); warp-aligned groups of lpb threads take spb
+    // consecutive segments of the same lpb lines
     const int lb = blk % max(g.nlb, 1);
-    const int seg = blk / max(g.nlb, 1);
-    const int line = lb * blockDim.x + threadIdx.x;
-    const bool active = blk < g.blocks && line < g.nlines;
+    const int sb = blk / max(g.nlb, 1);
+    const int sub = (int)threadIdx.x / g.lpb;
+    const int seg = sb * g.spb + sub;
+    const int line = lb * g.lpb + (int)threadIdx.x % g.lpb;
+    const bool active = blk < g.blocks && line < g.nlines && seg < g.nseg && sub < g.spb;
 
     if (active) {
         const int n = g.n, sw = A.sw;

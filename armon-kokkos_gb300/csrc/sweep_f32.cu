@@ -19,6 +19,11 @@ cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets,
     return launch_sweep_batch_t<float>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
 }
 
+int sweep_batch_blocks_per_sm_f32(int scheme, int proj, int block)
+{
+    return sweep_batch_blocks_per_sm_t<float>(scheme, proj, block);
+}
+
 cudaError_t launch_init_f32(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st)
 {
     int64_t blocks = (ncells + 255) / 256;

@@ -17,6 +17,11 @@ cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets
     return launch_sweep_batch_t<double>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
 }
 
+int sweep_batch_blocks_per_sm_f64(int scheme, int proj, int block)
+{
+    return sweep_batch_blocks_per_sm_t<double>(scheme, proj, block);
+}
+
 cudaError_t launch_init_f64(const InitArgs& a, int64_t ncells, const InitPtrs& p, cudaStream_t st)
 {
     int64_t blocks = (ncells + 255) / 256;

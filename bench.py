@@ -310,6 +310,130 @@ def run_gpu(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def plain_solve(A, spec, precision: int, graph: int) -> tuple[float, int]:
+    """One domain on the plain single-domain path (its own solver: init, upload of the initial
+    fields, time loop); returns the seconds of its time loop and its cell-updates."""
+    import torch
+
+    with A.Solver(spec.params(), precision=precision, cycles_per_graph=graph) as s:
+        s.init_test()
+        for k, a in spec.initial_state().items():
+            s.upload(k, a)
+        s.begin_loop()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.run()
+        secs = time.perf_counter() - t0
+        p, st = s.state()
+        assert st == 0
+        return secs, spec.nx * spec.ny * p.cycle
+
+
+def run_batch(args) -> None:
+    """Configuration 3: 256 uneven domains (seeded), FP64, each to t = 0.15 -- all of them in one
+    batch (one fused launch per pass, CUDA graphs) against the same domains one after another on the
+    plain single-domain path."""
+    import torch
+
+    import armon_gb300 as A
+    from armon_gb300 import workloads as W
+
+    specs = W.mixed_domains(args.domains, seed=2024)
+    torch.cuda.set_device(0)
+    # plain path (domains one at a time; the first is a warm-up)
+    plain_secs, plain_work = 0.0, 0
+    plain_solve(A, specs[0], 64, args.graph)
+    for sp in specs:
+        s_, w_ = plain_solve(A, sp, 64, args.graph)
+        plain_secs += s_
+        plain_work += w_
+    # batched
+    with A.Batch(precision=64, cycles_per_graph=8) as b:
+        ids = [b.add_sod(sp.params(), sp.sod_interface()) for sp in specs]
+        b.poll()
+        launches0 = b.kernel_launches
+        sampler = ClockSampler()
+        sampler.start()
+        t0 = time.perf_counter()
+        assert b.run() == 0
+        secs = time.perf_counter() - t0
+        clocks = sampler.stop()
+        launches = b.kernel_launches - launches0
+        waves, _ = b.schedule()
+        work = 0
+        for i, sp in zip(ids, specs):
+            p, st = b.state(i)
+            assert st == 0
+            work += sp.nx * sp.ny * p.cycle
+    assert work == plain_work
+    value = work / secs
+    cells = sum(sp.nx * sp.ny for sp in specs)
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 1, "warmup": 1,
+           "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{len(specs)} uneven Sod-interface domains (seed 2024), sides in "
+                                  "{64..1024}, GAD-minmod + euler_2nd, CFL 0.6, each to t = 0.15",
+                      "domains": len(specs), "cells": cells, "cell_updates": work,
+                      "step": "the whole batch run to completion (one fused launch per pass, 8-cycle CUDA graphs)"},
+           "plain": {"value": plain_work / plain_secs, "seconds": plain_secs,
+                     "path": "one Solver per domain, one after another (time loops only)"},
+           "batched_over_plain": value / (plain_work / plain_secs),
+           "schedule": {"waves": waves, "how": "autotuned online (CUDA-event timing of one graph batch per candidate)"},
+           "gpu_launches": launches, "clocks": clocks}
+    print(json.dumps(out), flush=True)
+
+
+def run_serve(args) -> None:
+    """Configuration 4: Poisson arrivals of Sod-interface solves (side lognormal(6, 0.6) clipped to
+    [128, 2048], FP64 or FP32 with p = 1/2, t_end ~ U(0.05, 0.2)) replayed in real time through the
+    server with a 150 GB state budget; p50/p99 time-to-solution and cell-updates/s."""
+    import torch
+
+    import armon_gb300 as A
+    from armon_gb300 import serving as S
+    from armon_gb300 import workloads as W
+
+    trace = W.serving_trace(n=args.requests, rate=args.rate, seed=7)
+    torch.cuda.set_device(0)
+    # warm-up: the kernels of both precisions
+    with A.Server(cycles_per_step=args.serve_cycles) as srv:
+        S.replay(srv, W.serving_trace(n=4, rate=1000.0, seed=1, side_range=(128, 128)))
+    with A.Server(memory_budget=150_000_000_000, cycles_per_step=args.serve_cycles) as srv:
+        sampler = ClockSampler()
+        sampler.start()
+        served, wall = S.replay(srv, trace)
+        clocks = sampler.stop()
+        launches = srv.kernel_launches
+    assert all(r.status == A.REQ_DONE for r in served)
+    work = sum(r.cells * r.cycles for r in served)
+    tts = [r.tts for r in served]
+    by_prec = {}
+    for prec in (64, 32):
+        t = [r.tts for r in served if r.precision == prec]
+        by_prec[str(prec)] = {"requests": len(t), "tts_p50_s": S.percentile(t, 0.5), "tts_p99_s": S.percentile(t, 0.99)}
+    # the plain path on a sample of the same requests, one solve at a time
+    sample = trace[:args.plain_sample]
+    p_secs, p_work = 0.0, 0
+    for r in sample:
+        s_, w_ = plain_solve(A, r.spec, r.spec.precision, args.graph)
+        p_secs += s_
+        p_work += w_
+    value = work / wall
+    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 1, "warmup": 1,
+           "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64+f32", "data": "synthetic",
+           "config": {"workload": f"{len(trace)} requests, Poisson arrivals at {args.rate}/s (seed 7), side "
+                                  "lognormal(6, 0.6) clipped to [128, 2048], FP64 or FP32 (p = 1/2), t_end ~ U(0.05, 0.2), "
+                                  "150 GB state budget",
+                      "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work},
+           "tts_p50_s": S.percentile(tts, 0.5), "tts_p99_s": S.percentile(tts, 0.99), "by_precision": by_prec,
+           "plain": {"value": p_work / p_secs, "seconds": p_secs, "sample": f"the first {len(sample)} requests",
+                     "path": "one Solver per request, one after another (time loops only)"},
+           "served_over_plain": value / (p_work / p_secs),
+           "gpu_launches": launches, "clocks": clocks}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -321,6 +445,13 @@ def main():
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
+                    help="single: the 4096^2 drop-in case (default); batch: 256 mixed domains; serve: a request trace")
+    ap.add_argument("--domains", type=int, default=256, help="--workload batch: domains")
+    ap.add_argument("--requests", type=int, default=2000, help="--workload serve: requests of the trace")
+    ap.add_argument("--rate", type=float, default=50.0, help="--workload serve: arrivals per second")
+    ap.add_argument("--serve-cycles", type=int, default=8, help="--workload serve: cycles per round")
+    ap.add_argument("--plain-sample", type=int, default=100, help="--workload serve: requests timed on the plain path")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -328,6 +459,10 @@ def main():
         args.size = 4096 if args.precision == 64 else 8192
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

@@ -147,8 +147,10 @@ typedef struct armon_batch_opts {
     int32_t precision;        /* 64 or 32: every domain of a batch has this precision */
     int32_t cycles_per_graph; /* cycles captured per CUDA graph launch (default 8) */
     int32_t block_lines;      /* lines (threads) per block: a multiple of 32, at most 128 (default 128) */
-    int32_t seg_len;          /* cells per thread along the sweep axis for every domain (0 = per domain) */
+    int32_t seg_len;          /* cells per thread along the sweep axis for every domain (0 = scheduled) */
     int64_t memory_budget;    /* bytes of domain state the batch may hold (0 = no limit) */
+    int32_t waves;            /* scheduled segments: block waves per launch to aim for (0 = autotuned) */
+    int32_t reserved;
 } armon_batch_opts;
 
 void armon_batch_opts_default(armon_batch_opts* o);
@@ -209,6 +211,10 @@ int armon_batch_download(armon_batch* b, int32_t id, int which, double* host);
 
 /* Frees a domain's state (stream-ordered) and its handle. */
 int armon_batch_remove(armon_batch* b, int32_t id);
+
+/* The batch schedule in use: block waves per launch the segments aim for (autotuned unless fixed
+ * by armon_batch_opts.waves or seg_len) and the blocks of the current launch table. */
+int armon_batch_schedule(armon_batch* b, int32_t* waves, int32_t* blocks);
 
 int32_t armon_batch_size(armon_batch* b);                /* domains held */
 int64_t armon_batch_bytes_in_use(armon_batch* b);

@@ -119,3 +119,26 @@ def test_batch_segment_choice_does_not_change_results():
         b.run()
         for k in FIELDS:
             assert np.array_equal(A.real_cells(b.params[i], b.download(i, k)), ref[k]), k
+
+
+def test_autotuned_schedule_keeps_results():
+    # enough cells for the tuner to time its candidates (one 8-cycle graph batch each)
+    specs = W.mixed_domains(6, seed=31, sides=(512, 768, 1024))
+    for s in specs:
+        s.t_end = 1.0
+    out = []
+    for waves in (0, 2):
+        with A.Batch(cycles_per_graph=8, waves=waves) as b:
+            ids = [b.add_sod(s.params(), s.sod_interface()) for s in specs]
+            b.run(cycle_limit=56)
+            w, blocks = b.schedule()
+            if waves == 0:
+                assert w in (2, 4, 8, 16, 64) and blocks > 0
+            else:
+                assert w == 2
+            out.append([{k: b.download(i, k) for k in FIELDS} for i in ids])
+            for i in ids:
+                assert b.state(i)[0].cycle == 56
+    for a, c in zip(*out):
+        for k in FIELDS:
+            assert np.array_equal(a[k], c[k]), k

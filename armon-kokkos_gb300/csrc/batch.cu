@@ -582,6 +582,11 @@ int armon_batch_poll(armon_batch* b, int32_t* running)
     return ARMON_OK;
 }
 
+int armon_batch_ready(armon_batch* b)
+{
+    return cudaStreamQuery(b->stream) == cudaSuccess ? 1 : 0;
+}
+
 int armon_batch_run(armon_batch* b, int32_t cycle_limit, int32_t* running)
 {
     int issued = 0, run = 0;

@@ -101,9 +101,12 @@ __global__ void cmp_check(uint64_t seed, int64_t n, unsigned long long* out)
         double x = from_bits(r1), y = (r3 & 3) == 0 ? from_bits(r1 ^ (r3 & 0x8000000000000000ull)) : from_bits(r2);
         if ((r3 & 12) == 4) y = from_bits(r1 + (r3 >> 60) - 8);     // neighbours
         if ((r3 & 48) == 16) x = from_bits(r3 & 0x8000000000000000ull);   // +-0
+        if ((r3 & 192) == 64) x = from_bits(0x3FF0000000000000ull + (r3 >> 61) - 4);   // around 1
         // neg_if is the multiply by -1 for non-NaN x (a NaN's sign and payload are not portable)
         bool ok = lt(x, y) == (x < y) && gt0(x) == (x > 0.0) &&
-                  (x != x || bits(neg_if(x, (r3 >> 7) & 1)) == bits((r3 >> 7) & 1 ? -x : x));
+                  (x != x || bits(neg_if(x, (r3 >> 7) & 1)) == bits((r3 >> 7) & 1 ? -x : x)) &&
+                  lt_pos(x, 0x3FF0000000000000ull) == (x < 1.0) && lt_pos(x, 0x4000000000000000ull) == (x < 2.0) &&
+                  lt_pos(y, 0x3FF0000000000000ull) == (y < 1.0);
         if (!ok && atomicAdd(&out[0], 1ull) == 0) {
             out[2] = bits(x);
             out[3] = bits(y);
@@ -168,6 +171,35 @@ __global__ void sqrt_check(uint64_t seed, int64_t n, unsigned long long* out)
     }
 }
 
+__global__ void mul_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1)), r3 = mix(r1 ^ r2);
+        double a, b;
+        switch (r3 & 7) {
+        case 0: a = from_bits(r1); b = from_bits(r2); break;                       // every class
+        case 1: {                                                                  // exact ties
+            const double qa = (double)((r1 >> 37) | 1), qb = (double)((r2 >> 37) | 1);   // 27-bit odd
+            a = ldexp(qa, (int)((r3 >> 8) % 200) - 100) * ((r3 & 8) ? -1.0 : 1.0);
+            b = ldexp(qb, (int)((r3 >> 16) % 200) - 100);
+            break;
+        }
+        case 2: a = normal_double(r1, 1023); b = normal_double(r2, 1023); break;   // overflow, underflow
+        case 3: a = normal_double(r1, 1023); b = from_bits(r2 & 0x800FFFFFFFFFFFFFull); break;   // subnormal, 0
+        default: a = normal_double(r1, 300); b = normal_double(r2, 300); break;    // normal products
+        }
+        const double s = mul(a, b), h = a * b;
+        if (!(bits(s) == bits(h) || (s != s && h != h)) && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = bits(a);
+            out[3] = bits(b);
+        }
+        // operands of the integer path: both normal
+        if ((uint32_t)((bits(a) >> 52) & 0x7FF) - 1u < 2046u && (uint32_t)((bits(b) >> 52) & 0x7FF) - 1u < 2046u)
+            atomicAdd(&out[1], 1ull);
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -175,7 +207,8 @@ extern "C" {
 // mode 0..6 (see operands) checks sfp::div against the hardware quotient; mode 100 checks lt,
 // gt0 and neg_if against the IEEE comparisons; mode 101 checks scale, half and twice against the
 // FP64 multiply by the power of two (out[3] = the exponent k of the first mismatch); mode 102
-// checks sqrt and absval against the hardware square root and fabs (out[3] = the soft root).  out[0] = mismatches, out[1] = fast-path operand
+// checks sqrt and absval against the hardware square root and fabs (out[3] = the soft root);
+// mode 103 checks mul against the FP64 multiply.  out[0] = mismatches, out[1] = fast-path operand
 // pairs, out[2..3] = the bits of the first mismatching operands.  Returns a cudaError_t.
 int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_host)
 {
@@ -186,6 +219,7 @@ int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_
     if (mode == 100) cmp_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 101) scale_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 102) sqrt_check<<<152 * 16, 256>>>(seed, n, out);
+    else if (mode == 103) mul_check<<<152 * 16, 256>>>(seed, n, out);
     else div_check<<<152 * 16, 256>>>(mode, seed, n, out);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out_host, out, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);

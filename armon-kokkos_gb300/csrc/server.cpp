@@ -13,6 +13,7 @@
 #include <deque>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "armon_gb300.h"
@@ -41,6 +42,7 @@ struct armon_server {
     armon_server_opts o{};
     Clock::time_point t0;
     std::map<BatchKey, armon_batch*> batches;
+    std::map<armon_batch*, bool> busy;  // cycles enqueued and not yet collected
     std::vector<Request> reqs;
     std::deque<int64_t> queue;        // waiting, in submission order
     std::vector<int64_t> running;     // on the device, loop not ended
@@ -173,27 +175,41 @@ int armon_server_step(armon_server* s, int32_t* in_flight, int32_t* queued)
 {
     int rc = admit(s);
     if (rc != ARMON_OK) return rc;
-    // every batch's cycles go to the device before the first wait
-    std::vector<armon_batch*> active;
+    // idle batches with running solves get their next cycles
     for (auto& kv : s->batches) {
+        armon_batch* b = kv.second;
+        if (s->busy[b]) continue;
         bool any = false;
         for (int64_t id : s->running)
-            if (s->reqs[(size_t)id].batch == kv.second) { any = true; break; }
+            if (s->reqs[(size_t)id].batch == b) { any = true; break; }
         if (!any) continue;
-        rc = armon_batch_enqueue_cycles(kv.second, s->o.cycles_per_step);
+        rc = armon_batch_enqueue_cycles(b, s->o.cycles_per_step);
         if (rc != ARMON_OK) return rc;
-        active.push_back(kv.second);
+        s->busy[b] = true;
     }
-    for (armon_batch* b : active) {
+    // wait for the first batch to finish its cycles, then collect every finished one
+    std::vector<armon_batch*> ready;
+    for (;;) {
+        bool any_busy = false;
+        for (auto& kv : s->busy) {
+            if (!kv.second) continue;
+            any_busy = true;
+            if (armon_batch_ready(kv.first)) ready.push_back(kv.first);
+        }
+        if (!ready.empty() || !any_busy) break;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    for (armon_batch* b : ready) {
         rc = armon_batch_poll(b, nullptr);
         if (rc != ARMON_OK) return rc;
+        s->busy[b] = false;
     }
     const double t = now(s);
     std::vector<int64_t> still;
     still.reserve(s->running.size());
     for (int64_t id : s->running) {
         Request& r = s->reqs[(size_t)id];
-        if (armon_batch_domain_done(r.batch, r.dom) != 1) {
+        if (s->busy[r.batch] || armon_batch_domain_done(r.batch, r.dom) != 1) {
             still.push_back(id);
             continue;
         }

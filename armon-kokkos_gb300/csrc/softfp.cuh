@@ -7,6 +7,7 @@
 //
 //   lt(x, y)      x < y  (false when either is NaN; -0 == +0)
 //   gt0(x)        x > 0
+//   lt_pos(x, c)  x < c for a positive constant c
 //   neg_if(x, c)  c ? -x : x  (a sign flip: what multiplying by -1 gives for non-NaN x)
 //   scale(x, k)   x * 2^k, exact (half(x) = x * 0.5, twice(x) = x * 2)
 //   absval(x)     |x|
@@ -67,6 +68,14 @@ __device__ __forceinline__ bool gt0(double x)
     return u > 0 && (uint64_t)u <= kInf;
 }
 
+// x < c for a constant c > 0 given by its bit pattern: the signed order of the patterns is the
+// IEEE order against a positive value, except for NaNs with the sign bit set.
+__device__ __forceinline__ bool lt_pos(double x, uint64_t c)
+{
+    const uint64_t u = bits(x);
+    return (int64_t)u < (int64_t)c && (u & kAbs) <= kInf;
+}
+
 // The sign-bit operations are written on the high word in inline PTX: a plain xor / and of the
 // bit pattern is recognised as an FP negation / absolute value, which can be materialised on the
 // FP64 pipe.
@@ -100,9 +109,41 @@ __device__ __forceinline__ double scale(double x, int k, double p2)
 __device__ __forceinline__ double half(double x) { return scale(x, -1, 0.5); }
 __device__ __forceinline__ double twice(double x) { return scale(x, 1, 2.0); }
 
-__device__ __forceinline__ double div(double a, double b)
+// The reciprocal of a divisor significand mb in (2^52, 2^53): V = 2^64 + v ~ 2^128 / d for
+// d = mb 2^11, from below.
+__device__ __forceinline__ uint64_t recip_v(uint64_t mb)
 {
-    const uint64_t ua = bits(a), ub = bits(b);
+    const uint64_t d = mb << 11;                                   // [2^63, 2^64)
+    const uint32_t top = (uint32_t)(d >> 40);                      // [2^23, 2^24)
+    const float fd = __uint_as_float(0x4B000000u | (top & 0x7FFFFFu));   // == top
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(fd));
+    const uint32_t urf = __float_as_uint(rf);
+    // rf in (2^-24, 2^-23]; rf * 2^88 = 2^64 (1 + m 2^-23) when rf < 2^-23.  The seed is lowered
+    // by 2^44 (2^-21 relative) so that it is below 2^128 / d.
+    uint64_t v;
+    if ((urf >> 23) >= 104u) {
+        v = 0xFFFFF00000000000ull;
+    } else {
+        const uint64_t m = (uint64_t)(urf & 0x7FFFFFu) << 41;
+        v = m > (1ull << 44) ? m - (1ull << 44) : 0;
+    }
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        // e = 2^128 - d (2^64 + v) >= 0; its high word, then V += V e / 2^128 (from below)
+        const uint64_t ph = __umul64hi(d, v);
+        const uint64_t pl = d * v;
+        const uint64_t eh = 0ull - d - ph - (pl != 0 ? 1ull : 0ull);
+        v = v + eh + __umul64hi(v, eh);
+    }
+    return v;
+}
+
+// a / b; the reciprocal comes from get_v(mb), called only on the integer path.
+template <class GetV>
+__device__ __forceinline__ double div_core(double a, double b, uint64_t ub, GetV get_v)
+{
+    const uint64_t ua = bits(a);
     const uint32_t ea = (uint32_t)(ua >> 52) & 0x7FFu;
     const uint32_t eb = (uint32_t)(ub >> 52) & 0x7FFu;
     const uint64_t sign = (ua ^ ub) & ~kAbs;
@@ -125,30 +166,8 @@ __device__ __forceinline__ double div(double a, double b)
         q = ma;
         r = 0;
     } else {
-        const uint64_t d = mb << 11;                                   // [2^63, 2^64)
-        const uint32_t top = (uint32_t)(d >> 40);                      // [2^23, 2^24)
-        const float fd = __uint_as_float(0x4B000000u | (top & 0x7FFFFFu));   // == top
-        float rf;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(fd));
-        const uint32_t urf = __float_as_uint(rf);
-        // V = 2^64 + v ~ 2^128 / d.  rf in (2^-24, 2^-23]; rf * 2^88 = 2^64 (1 + m 2^-23) when
-        // rf < 2^-23.  The seed is lowered by 2^44 (2^-21 relative) so that it is below 2^128 / d.
-        uint64_t v;
-        if ((urf >> 23) >= 104u) {
-            v = 0xFFFFF00000000000ull;
-        } else {
-            const uint64_t m = (uint64_t)(urf & 0x7FFFFFu) << 41;
-            v = m > (1ull << 44) ? m - (1ull << 44) : 0;
-        }
-#pragma unroll
-        for (int it = 0; it < 2; it++) {
-            // e = 2^128 - d (2^64 + v) >= 0; its high word, then V += V e / 2^128 (from below)
-            const uint64_t ph = __umul64hi(d, v);
-            const uint64_t pl = d * v;
-            const uint64_t eh = 0ull - d - ph - (pl != 0 ? 1ull : 0ull);
-            v = v + eh + __umul64hi(v, eh);
-        }
         // Q_est = floor((ma 2^63)(2^64 + v) / 2^128), dropping the low word of the dividend
+        const uint64_t v = get_v(mb);
         const uint64_t u1 = ma >> 1;
         q = u1 + __umul64hi(u1, v);
         r = (ma << 52) - q * mb;          // exact: the true remainder lies in [0, 2^56)
@@ -165,6 +184,65 @@ __device__ __forceinline__ double div(double a, double b)
     const bool up = r2 > mb || (r2 == mb && (q & 1));
     q += up ? 1ull : 0ull;
     return from_bits(sign + ((uint64_t)(e + 1022) << 52) + q);
+}
+
+__device__ __forceinline__ double div(double a, double b)
+{
+    return div_core(a, b, bits(b), [](uint64_t mb) { return recip_v(mb); });
+}
+
+// A divisor's reciprocal computed once for several quotients (when it is not a power of two and
+// the divisor is normal; div(a, R, b) is exact whatever R holds for other divisors).
+struct Recip {
+    uint64_t ub, v;
+};
+
+__device__ __forceinline__ Recip recip(double b)
+{
+    Recip R;
+    R.ub = bits(b);
+    const uint64_t mb = (R.ub & kMant) | kHidden;
+    const uint32_t eb = (uint32_t)(R.ub >> 52) & 0x7FFu;
+    R.v = (mb != kHidden && (eb - 1u) < 2046u) ? recip_v(mb) : 0;
+    return R;
+}
+
+__device__ __forceinline__ double div(double a, const Recip& R, double b)
+{
+    return div_core(a, b, R.ub, [&](uint64_t) { return R.v; });
+}
+
+// Multiplication (my own construction).  For normal operands with significands ma, mb in
+// [2^52, 2^53) the exact product ma mb lies in [2^104, 2^106); with both significands shifted to
+// bit 63, the high word of their 128-bit product holds its top 64 bits and the low word the rest.
+// The top 53 bits are the result significand, the next bit the rounding bit and everything below
+// it the sticky part; round to nearest, ties to even.  Zero operands give signed zeros; subnormal,
+// infinite and NaN operands and results outside the normal range take the FP64 multiply.
+__device__ __forceinline__ double mul(double a, double b)
+{
+    const uint64_t ua = bits(a), ub = bits(b);
+    const uint32_t ea = (uint32_t)(ua >> 52) & 0x7FFu;
+    const uint32_t eb = (uint32_t)(ub >> 52) & 0x7FFu;
+    const uint64_t sign = (ua ^ ub) & ~kAbs;
+    if ((ea - 1u) < 2046u && (eb - 1u) < 2046u) {
+        const uint64_t xa = ((ua & kMant) | kHidden) << 11;      // [2^63, 2^64)
+        const uint64_t xb = ((ub & kMant) | kHidden) << 11;
+        const uint64_t hi = __umul64hi(xa, xb);                  // [2^62, 2^64)
+        const bool lo_nz = xa * xb != 0;
+        const uint32_t top = (uint32_t)(hi >> 63);               // product >= 2^105
+        const uint32_t sh = 10 + top;
+        const uint64_t m = hi >> sh;                             // [2^52, 2^53)
+        const uint64_t rem = hi & ((1ull << sh) - 1);
+        const uint64_t halfw = 1ull << (sh - 1);
+        const bool up = rem > halfw || (rem == halfw && (lo_nz || (m & 1)));
+        const int e = (int)ea + (int)eb - 1023 + (int)top;      // biased exponent of the result
+        if ((unsigned)(e - 1) < 2046u) return from_bits(sign + ((uint64_t)(e - 1) << 52) + m + (up ? 1u : 0u));
+        return a * b;
+    }
+    if (((ua << 1) == 0 && (eb - 1u) < 2046u) || ((ub << 1) == 0 && (ea - 1u) < 2046u) ||
+        ((ua << 1) == 0 && (ub << 1) == 0))
+        return from_bits(sign);                                  // +-0 * normal or zero
+    return a * b;
 }
 
 // Square root (my own construction, in the manner of the division above).  A positive normal

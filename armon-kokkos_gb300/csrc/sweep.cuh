@@ -43,6 +43,13 @@
 #define ARMON_SOFT_FP64 1
 #endif
 
+// Stages whose FP64 products run on the integer pipes (sfp::mul), one bit per stage: 0 EOS,
+// 1 rho c and rho c u, 2 Godunov, 3 GAD, 4 face products, 5 Lagrange, 6 advection, 7 projection.
+// The FP64 pipe and the integer pipes then share the products; results are the same either way.
+#ifndef ARMON_SOFT_MUL
+#define ARMON_SOFT_MUL 0
+#endif
+
 // Blocks of 128 threads the compiler must fit on one SM (it caps registers accordingly).
 #ifndef ARMON_SWEEP_MIN_BLOCKS
 #define ARMON_SWEEP_MIN_BLOCKS 2
@@ -103,6 +110,13 @@ template <class T> struct GadDiff { T au, bu, ap, bp; };
 // give the IEEE results of the plain operators (for non-NaN operands where noted there).
 __device__ __forceinline__ double qdiv(double a, double b) { return ARMON_SOFT_FP64 ? sfp::div(a, b) : a / b; }
 __device__ __forceinline__ float qdiv(float a, float b) { return a / b; }
+// several quotients by one divisor share the divisor's reciprocal estimate
+struct QRecipD { sfp::Recip r; double b; };
+struct QRecipF { float b; };
+__device__ __forceinline__ QRecipD qrecip(double b) { return QRecipD{ARMON_SOFT_FP64 ? sfp::recip(b) : sfp::Recip{}, b}; }
+__device__ __forceinline__ QRecipF qrecip(float b) { return QRecipF{b}; }
+__device__ __forceinline__ double qdiv(double a, const QRecipD& R) { return ARMON_SOFT_FP64 ? sfp::div(a, R.r, R.b) : a / R.b; }
+__device__ __forceinline__ float qdiv(float a, const QRecipF& R) { return a / R.b; }
 __device__ __forceinline__ bool qlt(double a, double b) { return ARMON_SOFT_FP64 ? sfp::lt(a, b) : a < b; }
 __device__ __forceinline__ bool qlt(float a, float b) { return a < b; }
 __device__ __forceinline__ bool qgt0(double a) { return ARMON_SOFT_FP64 ? sfp::gt0(a) : a > 0.0; }
@@ -120,16 +134,26 @@ __device__ __forceinline__ double qscale(double x, int k, double p2) { return AR
 __device__ __forceinline__ float qscale(float x, int, float p2) { return x * p2; }
 __device__ __forceinline__ double qsqrt(double x) { return ARMON_SOFT_FP64 ? sfp::sqrt(x) : ::sqrt(x); }
 __device__ __forceinline__ float qsqrt(float x) { return sqrtf(x); }
+template <int G> __device__ __forceinline__ double qmul(double a, double b)
+{
+    return (ARMON_SOFT_FP64 && ((ARMON_SOFT_MUL >> G) & 1)) ? sfp::mul(a, b) : a * b;
+}
+template <int G> __device__ __forceinline__ float qmul(float a, float b) { return a * b; }
 // Kokkos::min / Kokkos::max: (b < a) ? b : a and (a < b) ? b : a
 template <class T> __device__ __forceinline__ T qmin(T a, T b) { return qlt(b, a) ? b : a; }
 template <class T> __device__ __forceinline__ T qmax(T a, T b) { return qlt(a, b) ? b : a; }
+// the same with a constant operand: max(0, x) and min(c, x) for c = 1 or 2
+template <class T> __device__ __forceinline__ T qmax0(T x) { return qgt0(x) ? x : T(0); }
+__device__ __forceinline__ double qmin_c(double c, uint64_t cbits, double x) { return ARMON_SOFT_FP64 ? (sfp::lt_pos(x, cbits) ? x : c) : (x < c ? x : c); }
+__device__ __forceinline__ float qmin_c(float c, uint64_t, float x) { return x < c ? x : c; }
+constexpr uint64_t kOneBits = 0x3FF0000000000000ull, kTwoBits = 0x4000000000000000ull;
 
 template <class T>
 __device__ __forceinline__ T limiter_fn(int L, T r)
 {
     // src/kernels/limiters.h:15-34
-    if (L == 1) return qmax(T(0), qmin(T(1), r));
-    if (L == 2) return qmax(qmax(T(0), qmin(T(1), qtwice(r))), qmin(T(2), r));
+    if (L == 1) return qmax0(qmin_c(T(1), kOneBits, r));
+    if (L == 2) return qmax(qmax0(qmin_c(T(1), kOneBits, qtwice(r))), qmin_c(T(2), kTwoBits, r));
     return T(1);
 }
 
@@ -140,10 +164,10 @@ __device__ __forceinline__ T slope_minmod(T d_m, T d_p, T r_m, T r_p)
     // differences of adjacent cells, shared by neighbouring faces).  s = copysign(1, D_u_p) is
     // +-1, so s * v is v with its sign flipped when D_u_p's sign bit is set (bit-identical to the
     // multiply for non-NaN v).
-    T D_u_p = r_p * d_p;
-    T D_u_m = r_m * d_m;
+    T D_u_p = qmul<6>(r_p, d_p);
+    T D_u_m = qmul<6>(r_m, d_m);
     const bool neg = qsignbit(D_u_p);
-    return qneg_if(qmax(T(0), qmin(qneg_if(D_u_p, neg), qneg_if(D_u_m, neg))), neg);
+    return qneg_if(qmax0(qmin(qneg_if(D_u_p, neg), qneg_if(D_u_m, neg))), neg);
 }
 
 template <class T>
@@ -162,9 +186,9 @@ template <class T>
 __device__ __forceinline__ void eos(CellIn<T>& c, T gamma, T gamma_m1)
 {
     // src/kernels/fluid_eos.cpp:18-21 (gamma_m1 = gamma - 1, computed once)
-    T e = c.E - qhalf(c.ua * c.ua + c.uo * c.uo);
-    c.p = gamma_m1 * c.rho * e;
-    c.c = qsqrt(qdiv(gamma * c.p, c.rho));
+    T e = c.E - qhalf(qmul<0>(c.ua, c.ua) + qmul<0>(c.uo, c.uo));
+    c.p = qmul<0>(qmul<0>(gamma_m1, c.rho), e);
+    c.c = qsqrt(qdiv(qmul<0>(gamma, c.p), c.rho));
 }
 
 template <class T>
@@ -173,8 +197,9 @@ __device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R
     // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i); rc_l * L.ua == L.rcu
     God<T> g;
     g.rcs = L.rc + R.rc;
-    g.us = qdiv(L.rcu + R.rcu + (L.p - R.p), g.rcs);
-    g.ps = qdiv(R.rc * L.p + L.rc * R.p + L.rc * R.rc * (L.ua - R.ua), g.rcs);
+    const auto inv = qrecip(g.rcs);
+    g.us = qdiv(L.rcu + R.rcu + (L.p - R.p), inv);
+    g.ps = qdiv(qmul<2>(R.rc, L.p) + qmul<2>(L.rc, R.p) + qmul<2>(qmul<2>(L.rc, R.rc), L.ua - R.ua), inv);
     return g;
 }
 
@@ -205,10 +230,10 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, 
     r_up = limiter_fn(L, r_up);
     r_pp = limiter_fn(L, r_pp);
     T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
-    T theta = qhalf(1 - qhalf(Gc.rcs) * qdiv(dt, Dm));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
+    T theta = qhalf(1 - qmul<3>(qhalf(Gc.rcs), qdiv(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
-    f.us = Gc.us + theta * (r_up * D0.bu - r_um * D0.au);
-    f.ps = Gc.ps + theta * (r_pp * D0.bp - r_pm * D0.ap);
+    f.us = Gc.us + qmul<3>(theta, qmul<3>(r_up, D0.bu) - qmul<3>(r_um, D0.au));
+    f.ps = Gc.ps + qmul<3>(theta, qmul<3>(r_pp, D0.bp) - qmul<3>(r_pm, D0.ap));
     return f;
 }
 
@@ -218,15 +243,15 @@ __device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0
     // src/kernels/euler_projection.cpp:9-22 for cell i (F0 = face i, F1 = face i+s)
     Lag<T> l;
     const T dm = C.dm;
-    l.W = dx + dt * (F1.us - F0.us);
+    l.W = dx + qmul<5>(dt, F1.us - F0.us);
     l.rho = qdiv(dm, l.W);
     T dtdm = qdiv(dt, dm);
-    l.ua = C.ua + dtdm * (F0.ps - F1.ps);
-    l.E = C.E + dtdm * (F0.psus - F1.psus);
+    l.ua = C.ua + qmul<5>(dtdm, F0.ps - F1.ps);
+    l.E = C.E + qmul<5>(dtdm, F0.psus - F1.psus);
     l.uo = C.uo;
-    l.rua = l.rho * l.ua;
-    l.ruo = l.rho * l.uo;
-    l.rE = l.rho * l.E;
+    l.rua = qmul<5>(l.rho, l.ua);
+    l.ruo = qmul<5>(l.rho, l.uo);
+    l.rE = qmul<5>(l.rho, l.E);
     l.c = C.c;
     return l;
 }
@@ -261,10 +286,10 @@ __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, 
     T slope_rE = slope_minmod(up ? d01.rE : d12.rE, up ? d12.rE : d23.rE, r_m, r_p);
     T length_factor = qdiv(Dx, two_Dx_l);
     Adv<T> a;
-    a.r = disp * ((up ? L1.rho : L2.rho) - slope_r * length_factor);
-    a.ra = disp * ((up ? L1.rua : L2.rua) - slope_ra * length_factor);
-    a.ro = disp * ((up ? L1.ruo : L2.ruo) - slope_ro * length_factor);
-    a.rE = disp * ((up ? L1.rE : L2.rE) - slope_rE * length_factor);
+    a.r = qmul<6>(disp, (up ? L1.rho : L2.rho) - qmul<6>(slope_r, length_factor));
+    a.ra = qmul<6>(disp, (up ? L1.rua : L2.rua) - qmul<6>(slope_ra, length_factor));
+    a.ro = qmul<6>(disp, (up ? L1.ruo : L2.ruo) - qmul<6>(slope_ro, length_factor));
+    a.rE = qmul<6>(disp, (up ? L1.rE : L2.rE) - qmul<6>(slope_rE, length_factor));
     return a;
 }
 
@@ -275,10 +300,10 @@ __device__ __forceinline__ Adv<T> advect1(const Flux<T>& Fk, const Lag<T>& Lm, c
     T disp = Fk.dtus;
     bool up = qgt0(disp);
     Adv<T> a;
-    a.r = disp * (up ? Lm.rho : Lk.rho);
-    a.ra = disp * (up ? Lm.rua : Lk.rua);
-    a.ro = disp * (up ? Lm.ruo : Lk.ruo);
-    a.rE = disp * (up ? Lm.rE : Lk.rE);
+    a.r = qmul<6>(disp, up ? Lm.rho : Lk.rho);
+    a.ra = qmul<6>(disp, up ? Lm.rua : Lk.rua);
+    a.ro = qmul<6>(disp, up ? Lm.ruo : Lk.ruo);
+    a.rE = qmul<6>(disp, up ? Lm.rE : Lk.rE);
     return a;
 }
 
@@ -437,8 +462,8 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                         A.gmat[idx] = (1 + A.gamma) / 2;
                     }
                 }
-                c.rc = c.rho * c.c;
-                c.rcu = c.rc * c.ua;
+                c.rc = qmul<1>(c.rho, c.c);
+                c.rcu = qmul<1>(c.rc, c.ua);
                 c.dm = mul_dx(c.rho, g);
                 C2 = c;
             }
@@ -457,8 +482,8 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 } else {
                     f.us = G2.us; f.ps = G2.ps;
                 }
-                f.psus = f.ps * f.us;
-                f.dtus = dt * f.us;
+                f.psus = qmul<4>(f.ps, f.us);
+                f.dtus = qmul<4>(dt, f.us);
                 F4 = f;
             }
             // ---- Lagrange update of cell j = t - LAG_L ----
@@ -482,12 +507,13 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             if (mm >= a0) {
                 const Lag<T>& Lc = kE2 ? L1 : L2;
                 // src/kernels/euler_projection.cpp:36-46
-                T dXr = Lc.W * Lc.rho;
+                T dXr = qmul<7>(Lc.W, Lc.rho);
                 T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
-                T tmp_ra = div_dx(dXr * Lc.ua - (A1.ra - A0.ra), g);
-                T tmp_ro = div_dx(dXr * Lc.uo - (A1.ro - A0.ro), g);
-                T tmp_rE = div_dx(dXr * Lc.E - (A1.rE - A0.rE), g);
-                T ua = qdiv(tmp_ra, tmp_rho), uo = qdiv(tmp_ro, tmp_rho), E = qdiv(tmp_rE, tmp_rho);
+                T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (A1.ra - A0.ra), g);
+                T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (A1.ro - A0.ro), g);
+                T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (A1.rE - A0.rE), g);
+                const auto inv_rho = qrecip(tmp_rho);
+                T ua = qdiv(tmp_ra, inv_rho), uo = qdiv(tmp_ro, inv_rho), E = qdiv(tmp_rE, inv_rho);
                 const int64_t idx = base + (int64_t)mm * s;
                 out[0][idx] = tmp_rho;
                 out[axis == 0 ? 1 : 2][idx] = ua;

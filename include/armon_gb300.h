@@ -201,6 +201,9 @@ int armon_batch_run(armon_batch* b, int32_t cycle_limit, int32_t* running);
 /* Reads back all domain states; *running receives how many loops are still running. */
 int armon_batch_poll(armon_batch* b, int32_t* running);
 
+/* 1 when everything enqueued on the batch's stream has finished (a poll would not wait), else 0. */
+int armon_batch_ready(armon_batch* b);
+
 /* State of one domain as of the last poll / run (cycle, time, dts in p; status 0 running or done,
  * 1 invalid dt). */
 int armon_batch_domain_state(armon_batch* b, int32_t id, armon_params* p, int32_t* status);
@@ -259,8 +262,11 @@ void armon_server_destroy(armon_server* s);
 int armon_server_submit(armon_server* s, const armon_params* p, int32_t precision, const armon_sod_interface* sod,
                         int64_t* req);
 
-/* One round: admission, cycles_per_step cycles of every running solve, retirement of the solves
- * that finished.  *in_flight / *queued (may be NULL) receive the running / waiting requests. */
+/* One round: admission; every batch with running solves and no cycles in progress gets
+ * cycles_per_step more; then waits until at least one batch in progress has finished its cycles,
+ * and retires the solves of the finished batches whose loop ended.  Batches proceed independently
+ * (a fast batch is not held back by a slow one).  *in_flight / *queued (may be NULL) receive the
+ * running / waiting requests. */
 int armon_server_step(armon_server* s, int32_t* in_flight, int32_t* queued);
 
 /* Pops the next finished (done or failed) request not yet reported: returns 1 and sets *req, or 0. */

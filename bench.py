@@ -55,15 +55,20 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profiled_traffic() -> float | None:
-    """DRAM bytes per sweep launch from the committed ncu summary, scaled to this workload."""
+def profiled(key: str) -> float | None:
+    """A per-cell figure from the committed ncu summary (profiles/sweep_f64_sod_circ.md)."""
     path = os.path.join(ROOT, "profiles", "sweep_f64_sod_circ.md")
     try:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(r"traffic_bytes_per_cell_per_pass:\s*([0-9.eE+-]+)", txt)
+    m = re.search(key + r":\s*([0-9.eE+-]+)", txt)
     return float(m.group(1)) if m else None
+
+
+def profiled_traffic() -> float | None:
+    """DRAM bytes per cell and sweep launch (scaled to the workload by the caller)."""
+    return profiled("traffic_bytes_per_cell_per_pass")
 
 
 class ClockSampler:
@@ -118,6 +123,25 @@ class ClockSampler:
         reasons = sorted({names[k] for r in rs for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rs[0][2]), "reasons": reasons,
                 "samples": len(rs), "power_w_median": statistics.median(float(r[3]) for r in rs)}
+
+
+def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None) -> dict | None:
+    """The FP64 pipe as the bound: FP64 operations per cell and launch (ncu's DADD + DMUL + DFMA
+    counts, profiles/) over the pipe's peak, 2 per SM per cycle (ncu's peak_sustained) at the SM
+    clock sampled during the timed region."""
+    import torch
+
+    ops = profiled("fp64_ops_per_cell_per_pass")
+    if not ops:
+        return None
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = 2.0 * sms * mhz * 1e6
+    achieved = ops * cells * 2 / s_per_cycle
+    return {"bound": "fp64", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G FP64 op/s",
+            "frac": achieved / peak, "ops_per_cell_per_launch": ops,
+            "note": "divisions, square roots and compares run on the integer pipes (exact), so only "
+                    "additions and multiplications count here"}
 
 
 def dist_info() -> tuple[int, int, int]:
@@ -297,7 +321,8 @@ def run_gpu(args) -> None:
                             "kernel": "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)"
                                       % ("double" if prec == 64 else "float"),
                             "algorithmic_bytes_per_launch": bpc / 2 * cells,
-                            "note": "FP64 arithmetic bound: see fp64_pipe in profiles/"},
+                            "note": "not HBM-bound: the FP64 pipe and integer latency bound the pass (fp64_roofline, profiles/)"},
+               "fp64_roofline": fp64_roofline(cells, ms_max / 1e3 / K, clocks) if prec == 64 else None,
                "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
                        "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,
                        "host_arrays": "FP64 (converted to the solver's precision inside the call)",

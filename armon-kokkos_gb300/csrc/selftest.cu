@@ -200,6 +200,31 @@ __global__ void mul_check(uint64_t seed, int64_t n, unsigned long long* out)
     }
 }
 
+// The division's quotient estimate against exact 128-bit arithmetic: the remainder
+// ma 2^52 - q mb must lie in [0, 2 mb) (one correction step then gives the quotient).
+__global__ void quot_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1)), r3 = mix(r1 ^ r2);
+        uint64_t mb = (r2 & kMant) | kHidden;
+        if ((r3 & 15) == 0) mb = kHidden + 1;                       // just above a power of two
+        if ((r3 & 15) == 1) mb = (kHidden << 1) - 1;                // just below the next
+        if (mb == kHidden) mb += 1;
+        uint64_t ma = (r1 & kMant) | kHidden;
+        if ((r3 >> 4) & 1) ma <<= 1;                                // the doubled dividend
+        if ((r3 & 0xE0) == 0x20) ma = (r3 >> 8) & 1 ? (kHidden << 2) - 1 : kHidden;
+        const uint64_t q = quot_estimate(ma, recip_v(mb));
+        const unsigned __int128 num = (unsigned __int128)ma << 52;
+        const unsigned __int128 qm = (unsigned __int128)q * mb;
+        const bool ok = qm <= num && num - qm < 2 * (unsigned __int128)mb;
+        if (!ok && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = ma;
+            out[3] = mb;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -208,7 +233,8 @@ extern "C" {
 // gt0 and neg_if against the IEEE comparisons; mode 101 checks scale, half and twice against the
 // FP64 multiply by the power of two (out[3] = the exponent k of the first mismatch); mode 102
 // checks sqrt and absval against the hardware square root and fabs (out[3] = the soft root);
-// mode 103 checks mul against the FP64 multiply.  out[0] = mismatches, out[1] = fast-path operand
+// mode 103 checks mul against the FP64 multiply; mode 104 checks the division's quotient
+// estimate against 128-bit arithmetic (out[2..3] = ma, mb of the first miss).  out[0] = mismatches, out[1] = fast-path operand
 // pairs, out[2..3] = the bits of the first mismatching operands.  Returns a cudaError_t.
 int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_host)
 {
@@ -220,6 +246,7 @@ int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_
     else if (mode == 101) scale_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 102) sqrt_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 103) mul_check<<<152 * 16, 256>>>(seed, n, out);
+    else if (mode == 104) quot_check<<<152 * 16, 256>>>(seed, n, out);
     else div_check<<<152 * 16, 256>>>(mode, seed, n, out);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out_host, out, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);

@@ -20,7 +20,7 @@
 // with a reciprocal of d = mb * 2^11: an FP32 seed (rcp.approx of the top 24 bits), biased below
 // the true value, then two Newton steps y <- y + y (1 - d y) in 64-bit fixed point, each of which
 // keeps the estimate below 2^128 / d; then Q_est = floor(U * V / 2^128) for U = ma * 2^63.  The
-// remainder is computed exactly in 64 bits and Q_est is raised while R >= mb.  If R still is not
+// remainder is computed exactly in 64 bits and Q_est is raised once if R >= mb.  If R still is not
 // in [0, mb) -- which the error bounds exclude -- the hardware division is used, so a fast-path
 // result always satisfies ma * 2^52 = Q * mb + R with 0 <= R < mb, i.e. Q is exact.  Zero
 // dividends are handled; subnormal, infinite and NaN operands and quotients outside the normal
@@ -139,6 +139,15 @@ __device__ __forceinline__ uint64_t recip_v(uint64_t mb)
     return v;
 }
 
+// The quotient estimate of significands ma in [2^52, 2^54) and mb (reciprocal V = 2^64 + v):
+// floor(x (2^64 + v) / 2^74) for x = ma 2^9 (< 2^63).  V lies within 2^-62 below 2^128 / d, so the
+// estimate is floor(ma 2^52 / mb) or one less.
+__device__ __forceinline__ uint64_t quot_estimate(uint64_t ma, uint64_t v)
+{
+    const uint64_t x = ma << 9;
+    return (x + __umul64hi(x, v)) >> 10;
+}
+
 // a / b; the reciprocal comes from get_v(mb), called only on the integer path.
 template <class GetV>
 __device__ __forceinline__ double div_core(double a, double b, uint64_t ub, GetV get_v)
@@ -166,17 +175,12 @@ __device__ __forceinline__ double div_core(double a, double b, uint64_t ub, GetV
         q = ma;
         r = 0;
     } else {
-        // Q_est = floor((ma 2^63)(2^64 + v) / 2^128), dropping the low word of the dividend
-        const uint64_t v = get_v(mb);
-        const uint64_t u1 = ma >> 1;
-        q = u1 + __umul64hi(u1, v);
-        r = (ma << 52) - q * mb;          // exact: the true remainder lies in [0, 2^56)
-#pragma unroll
-        for (int it = 0; it < 3; it++) {
-            const bool up = r >= mb;
-            r = up ? r - mb : r;
-            q = up ? q + 1 : q;
-        }
+        // Q_est is Q or Q - 1, and one correction step makes it Q
+        q = quot_estimate(ma, get_v(mb));
+        r = (ma << 52) - q * mb;          // exact: the true remainder lies in [0, 2 mb)
+        const bool up1 = r >= mb;
+        r = up1 ? r - mb : r;
+        q = up1 ? q + 1 : q;
         if (r >= mb) return a / b;        // outside the error bounds: the hardware decides
     }
     // round to nearest, ties to even, on the exact remainder

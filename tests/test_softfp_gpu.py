@@ -11,7 +11,8 @@ pytestmark = pytest.mark.gpu
 MODES = {0: "random normal operands", 1: "random bit patterns (zeros, subnormals, inf, NaN)",
          2: "quotients near a rounding midpoint", 3: "exact quotients", 4: "power-of-two divisors",
          5: "zero dividends, extreme exponents", 6: "solver-like magnitudes", 100: "lt / gt0 / neg_if / lt_pos",
-         101: "scale / half / twice", 102: "sqrt / absval", 103: "mul"}
+         101: "scale / half / twice", 102: "sqrt / absval", 103: "mul",
+         104: "division quotient estimate within one"}
 
 
 def selftest(mode, n, seed):

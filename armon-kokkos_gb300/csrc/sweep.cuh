@@ -50,6 +50,21 @@
 #define ARMON_SOFT_MUL 0
 #endif
 
+// Division sites that use the FP64 pipe's IEEE division instead of the integer-pipe one, one bit
+// per site: 0 EOS gamma p / rho, 1 Godunov, 2 GAD ratios, 3 GAD dt / Dm, 4 Lagrange dm / W,
+// 5 Lagrange dt / dm, 6 advection ratios, 7 advection length factor, 8 projection, 9 EOS sqrt.
+// Both give the same results.
+#ifndef ARMON_HW_DIV
+#define ARMON_HW_DIV 0
+#endif
+
+// Unrolling of the march along a line (the pipeline windows then rotate by register renaming
+// instead of copies).
+#ifndef ARMON_SWEEP_UNROLL
+#define ARMON_SWEEP_UNROLL 1
+#endif
+constexpr int kSweepUnroll = ARMON_SWEEP_UNROLL;
+
 // Blocks of 128 threads the compiler must fit on one SM (it caps registers accordingly).
 #ifndef ARMON_SWEEP_MIN_BLOCKS
 #define ARMON_SWEEP_MIN_BLOCKS 2
@@ -117,6 +132,13 @@ __device__ __forceinline__ QRecipD qrecip(double b) { return QRecipD{ARMON_SOFT_
 __device__ __forceinline__ QRecipF qrecip(float b) { return QRecipF{b}; }
 __device__ __forceinline__ double qdiv(double a, const QRecipD& R) { return ARMON_SOFT_FP64 ? sfp::div(a, R.r, R.b) : a / R.b; }
 __device__ __forceinline__ float qdiv(float a, const QRecipF& R) { return a / R.b; }
+// the same per division site S (ARMON_HW_DIV)
+template <int S> __device__ __forceinline__ double qdiv_at(double a, double b) { return ((ARMON_HW_DIV >> S) & 1) ? a / b : qdiv(a, b); }
+template <int S> __device__ __forceinline__ float qdiv_at(float a, float b) { return a / b; }
+template <int S> __device__ __forceinline__ QRecipD qrecip_at(double b) { return ((ARMON_HW_DIV >> S) & 1) ? QRecipD{sfp::Recip{}, b} : qrecip(b); }
+template <int S> __device__ __forceinline__ QRecipF qrecip_at(float b) { return qrecip(b); }
+template <int S> __device__ __forceinline__ double qdiv_at(double a, const QRecipD& R) { return ((ARMON_HW_DIV >> S) & 1) ? a / R.b : qdiv(a, R); }
+template <int S> __device__ __forceinline__ float qdiv_at(float a, const QRecipF& R) { return a / R.b; }
 __device__ __forceinline__ bool qlt(double a, double b) { return ARMON_SOFT_FP64 ? sfp::lt(a, b) : a < b; }
 __device__ __forceinline__ bool qlt(float a, float b) { return a < b; }
 __device__ __forceinline__ bool qgt0(double a) { return ARMON_SOFT_FP64 ? sfp::gt0(a) : a > 0.0; }
@@ -188,7 +210,8 @@ __device__ __forceinline__ void eos(CellIn<T>& c, T gamma, T gamma_m1)
     // src/kernels/fluid_eos.cpp:18-21 (gamma_m1 = gamma - 1, computed once)
     T e = c.E - qhalf(qmul<0>(c.ua, c.ua) + qmul<0>(c.uo, c.uo));
     c.p = qmul<0>(qmul<0>(gamma_m1, c.rho), e);
-    c.c = qsqrt(qdiv(qmul<0>(gamma, c.p), c.rho));
+    const T q = qdiv_at<0>(qmul<0>(gamma, c.p), c.rho);
+    c.c = ((ARMON_HW_DIV >> 9) & 1) ? sqrt(q) : qsqrt(q);
 }
 
 template <class T>
@@ -197,9 +220,9 @@ __device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R
     // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i); rc_l * L.ua == L.rcu
     God<T> g;
     g.rcs = L.rc + R.rc;
-    const auto inv = qrecip(g.rcs);
-    g.us = qdiv(L.rcu + R.rcu + (L.p - R.p), inv);
-    g.ps = qdiv(qmul<2>(R.rc, L.p) + qmul<2>(L.rc, R.p) + qmul<2>(qmul<2>(L.rc, R.rc), L.ua - R.ua), inv);
+    const auto inv = qrecip_at<1>(g.rcs);
+    g.us = qdiv_at<1>(L.rcu + R.rcu + (L.p - R.p), inv);
+    g.ps = qdiv_at<1>(qmul<2>(R.rc, L.p) + qmul<2>(L.rc, R.p) + qmul<2>(qmul<2>(L.rc, R.rc), L.ua - R.ua), inv);
     return g;
 }
 
@@ -221,16 +244,16 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, 
     // src/kernels/acoustic.cpp:40-88 for face i (between cells i-s and i), with the differences
     // of faces i-s (Dm1), i (D0), i+s (Dp1):  Gp.us - Cr.ua == Dp1.au, Gc.us - Cl.ua == D0.au,
     // Cl.ua - Gm.us == Dm1.bu, Cr.ua - Gc.us == D0.bu (the same for p).
-    T r_um = qdiv(Dp1.au, D0.au + T(1e-6));
-    T r_pm = qdiv(Dp1.ap, D0.ap + T(1e-6));
-    T r_up = qdiv(Dm1.bu, D0.bu + T(1e-6));
-    T r_pp = qdiv(Dm1.bp, D0.bp + T(1e-6));
+    T r_um = qdiv_at<2>(Dp1.au, D0.au + T(1e-6));
+    T r_pm = qdiv_at<2>(Dp1.ap, D0.ap + T(1e-6));
+    T r_up = qdiv_at<2>(Dm1.bu, D0.bu + T(1e-6));
+    T r_pp = qdiv_at<2>(Dm1.bp, D0.bp + T(1e-6));
     r_um = limiter_fn(L, r_um);
     r_pm = limiter_fn(L, r_pm);
     r_up = limiter_fn(L, r_up);
     r_pp = limiter_fn(L, r_pp);
     T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
-    T theta = qhalf(1 - qmul<3>(qhalf(Gc.rcs), qdiv(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
+    T theta = qhalf(1 - qmul<3>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
     f.us = Gc.us + qmul<3>(theta, qmul<3>(r_up, D0.bu) - qmul<3>(r_um, D0.au));
     f.ps = Gc.ps + qmul<3>(theta, qmul<3>(r_pp, D0.bp) - qmul<3>(r_pm, D0.ap));
@@ -244,8 +267,8 @@ __device__ __forceinline__ Lag<T> lagrange(const CellIn<T>& C, const Flux<T>& F0
     Lag<T> l;
     const T dm = C.dm;
     l.W = dx + qmul<5>(dt, F1.us - F0.us);
-    l.rho = qdiv(dm, l.W);
-    T dtdm = qdiv(dt, dm);
+    l.rho = qdiv_at<4>(dm, l.W);
+    T dtdm = qdiv_at<5>(dt, dm);
     l.ua = C.ua + qmul<5>(dtdm, F0.ps - F1.ps);
     l.E = C.E + qmul<5>(dtdm, F0.psus - F1.psus);
     l.uo = C.uo;
@@ -278,13 +301,13 @@ __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, 
     T Dx = qneg_if(dx + (up ? qneg_if(Fm.dtus, true) : Fp.dtus), up);
     const T Dx_l = up ? L1.W : L2.W;
     const T two_Dx_l = qtwice(Dx_l);
-    T r_m = qdiv(two_Dx_l, up ? s01 : s12);    // 2 Dx_l / (Dx_l + Dx_lm)
-    T r_p = qdiv(two_Dx_l, up ? s12 : s23);    // 2 Dx_l / (Dx_l + Dx_lp)
+    T r_m = qdiv_at<6>(two_Dx_l, up ? s01 : s12);    // 2 Dx_l / (Dx_l + Dx_lm)
+    T r_p = qdiv_at<6>(two_Dx_l, up ? s12 : s23);    // 2 Dx_l / (Dx_l + Dx_lp)
     T slope_r = slope_minmod(up ? d01.r : d12.r, up ? d12.r : d23.r, r_m, r_p);
     T slope_ra = slope_minmod(up ? d01.ra : d12.ra, up ? d12.ra : d23.ra, r_m, r_p);
     T slope_ro = slope_minmod(up ? d01.ro : d12.ro, up ? d12.ro : d23.ro, r_m, r_p);
     T slope_rE = slope_minmod(up ? d01.rE : d12.rE, up ? d12.rE : d23.rE, r_m, r_p);
-    T length_factor = qdiv(Dx, two_Dx_l);
+    T length_factor = qdiv_at<7>(Dx, two_Dx_l);
     Adv<T> a;
     a.r = qmul<6>(disp, (up ? L1.rho : L2.rho) - qmul<6>(slope_r, length_factor));
     a.ra = qmul<6>(disp, (up ? L1.rua : L2.rua) - qmul<6>(slope_ra, length_factor));
@@ -422,6 +445,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         T s01{}, s12{}, s23{};               // W(j) + W(j+1)
         Adv<T> A0{}, A1{};
 
+#pragma unroll kSweepUnroll
         for (int t = t0; t <= t1; ++t) {
             // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
             C0 = C1; C1 = C2;
@@ -512,8 +536,8 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (A1.ra - A0.ra), g);
                 T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (A1.ro - A0.ro), g);
                 T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (A1.rE - A0.rE), g);
-                const auto inv_rho = qrecip(tmp_rho);
-                T ua = qdiv(tmp_ra, inv_rho), uo = qdiv(tmp_ro, inv_rho), E = qdiv(tmp_rE, inv_rho);
+                const auto inv_rho = qrecip_at<8>(tmp_rho);
+                T ua = qdiv_at<8>(tmp_ra, inv_rho), uo = qdiv_at<8>(tmp_ro, inv_rho), E = qdiv_at<8>(tmp_rE, inv_rho);
                 const int64_t idx = base + (int64_t)mm * s;
                 out[0][idx] = tmp_rho;
                 out[axis == 0 ? 1 : 2][idx] = ua;

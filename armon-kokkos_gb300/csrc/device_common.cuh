@@ -100,7 +100,8 @@ __host__ __device__ inline int passes_per_cycle(int32_t splitting)
 // Kokkos::min chain (kmin(acc, kmin(dx/ax, dy/ay)), identity DBL_MAX) treats them.
 struct DtAcc {
     double ax, ay;
-    __device__ __forceinline__ void init() { ax = 0.0; ay = 0.0; }
+    uint32_t fx, fy;        // the FP32 variant's maxima, as float bit patterns (finish() folds them in)
+    __device__ __forceinline__ void init() { ax = 0.0; ay = 0.0; fx = 0; fy = 0; }
     __device__ __forceinline__ void add(double u, double v, double c)
     {
         // kmax of non-negative values: for sign-clear, non-NaN doubles the IEEE order is the
@@ -123,16 +124,23 @@ struct DtAcc {
         }
     }
     __device__ __forceinline__ void merge(double ox, double oy) { ax = kmax(ax, ox); ay = kmax(ay, oy); }
-    // The same for FP32 fields: the per-cell speeds in FP32 (FP64 arithmetic per cell would put
-    // the FP32 variant on GB300's 1/64-rate FP64 pipe), the maxima, dt and the step logic in FP64.
+    // The same for FP32 fields: the per-cell speeds in FP32 and their maxima as float bit patterns
+    // (the unsigned order of non-negative floats; FP64 arithmetic per cell would put the FP32
+    // variant on GB300's 1/64-rate FP64 pipe); float -> double is exact and monotone, so folding the
+    // maxima into FP64 once gives what a per-cell FP64 maximum gives.  dt and the step logic are FP64.
     __device__ __forceinline__ void add(float u, float v, float c)
     {
-        float mx = kmax(fabsf(u + c), fabsf(u - c));
-        float my = kmax(fabsf(v + c), fabsf(v - c));
+        const float mx = kmax(fabsf(u + c), fabsf(u - c));
+        const float my = kmax(fabsf(v + c), fabsf(v - c));
         if (mx == mx) {
-            ax = kmax(ax, double(mx));
-            if (my == my) ay = kmax(ay, double(my));
+            fx = max(fx, __float_as_uint(mx));
+            if (my == my) fy = max(fy, __float_as_uint(my));
         }
+    }
+    __device__ __forceinline__ void finish()
+    {
+        ax = kmax(ax, double(__uint_as_float(fx)));
+        ay = kmax(ay, double(__uint_as_float(fy)));
     }
 };
 

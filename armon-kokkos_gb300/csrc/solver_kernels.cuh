@@ -83,6 +83,7 @@ __global__ void begin_kernel(BeginArgs a)
         gmat[idx] = (1 + gamma) / 2;
         acc.add(umat[idx], vmat[idx], c);
     }
+    acc.finish();
     double gx, gy;
     if (grid_dt_maxima(acc, a.partials, &a.state->counter, &gx, &gy)) {
         StepState s{};

@@ -65,10 +65,16 @@
 #endif
 constexpr int kSweepUnroll = ARMON_SWEEP_UNROLL;
 
-// Blocks of 128 threads the compiler must fit on one SM (it caps registers accordingly).
+// Blocks of 128 threads the compiler must fit on one SM (it caps registers accordingly): the FP64
+// pass keeps its ~250 registers (two blocks), the FP32 pass fits three (four spill, and measured
+// slower).
 #ifndef ARMON_SWEEP_MIN_BLOCKS
 #define ARMON_SWEEP_MIN_BLOCKS 2
 #endif
+#ifndef ARMON_SWEEP_MIN_BLOCKS_F32
+#define ARMON_SWEEP_MIN_BLOCKS_F32 3
+#endif
+template <class T> constexpr int sweep_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_SWEEP_MIN_BLOCKS; }
 
 namespace armon {
 
@@ -552,12 +558,15 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         }
     }
 
-    if constexpr (LAST) commit_cycle(A, acc, st, cd, blk, nblk);
+    if constexpr (LAST) {
+        acc.finish();
+        commit_cycle(A, acc, st, cd, blk, nblk);
+    }
 }
 
 // One domain: the whole grid works on it.
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128, ARMON_SWEEP_MIN_BLOCKS) sweep_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_kernel(const SweepArgs<T> A)
 {
     sweep_domain<T, SCHEME, PROJ, LAST>(A, blockIdx.x, gridDim.x, A.pass);
 }
@@ -566,7 +575,7 @@ __global__ void __launch_bounds__(128, ARMON_SWEEP_MIN_BLOCKS) sweep_kernel(cons
 // grid (enough for its larger axis); each domain keeps its own step state, so dt, time and cycle
 // advance per domain and a finished domain's blocks return at once.
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128, ARMON_SWEEP_MIN_BLOCKS) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
+__global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
                                                           const int* __restrict__ offsets, int ndom, int pass)
 {
     const int b = blockIdx.x;

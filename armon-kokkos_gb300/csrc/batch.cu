@@ -183,7 +183,7 @@ int rebuild_t(armon_batch* b)
         const int fixed = d.seg_len > 0 ? d.seg_len : b->o.seg_len;
         const int forced[2] = {fixed > 0 ? fixed : sched[k][0], fixed > 0 ? fixed : sched[k][1]};
         int nb = make_sweep_args<T>(d.p, b->npass, b->o.block_lines, b->sm_count, forced, buffers<T>(d),
-                                    b->d_states + b->table[k], d.partials, 1, args[k]);
+                                    b->d_states + b->table[k], d.partials, 0, args[k]);
         if (nb > d.npartials) { set_error("domain needs more partial slots than allotted"); return ARMON_ERR_STATE; }
         offsets[k + 1] = offsets[k] + nb;
     }

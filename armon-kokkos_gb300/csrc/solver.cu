@@ -155,7 +155,7 @@ void armon_solver_opts_default(armon_solver_opts* o)
     std::memset(o, 0, sizeof(*o));
     o->precision = 64;
     o->cycles_per_graph = 16;
-    o->materialize_eos = 1;
+    o->materialize_eos = 0;
 }
 
 static int solver_create(const armon_params* p, const armon_solver_opts* opts, double* const* borrowed, void* stream,

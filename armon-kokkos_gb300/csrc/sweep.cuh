@@ -106,7 +106,7 @@ struct SweepArgs {
     int32_t limiter;                  // 0 None, 1 Minmod, 2 Superbee
     int32_t pass;                     // pass index within the cycle
     int32_t npass;                    // passes per cycle
-    int32_t write_eos;                // materialise p, c, g of the real cells
+    int32_t write_eos;                // materialise p, c, g of the real cells on every pass (else on the last)
     int32_t pad;
     T gamma;
     T* buf[2][4];                     // two state sets: rho, umat, vmat, Emat
@@ -486,7 +486,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                     c.c = A.cmat[idx];
                 } else {
                     eos(c, A.gamma, gamma_m1);
-                    if (m == t && t >= a0 && t < b0 && A.write_eos) {   // owned real cell: what update_EOS stores
+                    if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
                         A.pmat[idx] = c.p;
                         A.cmat[idx] = c.c;
                         A.gmat[idx] = (1 + A.gamma) / 2;

@@ -85,8 +85,9 @@ typedef struct armon_solver_opts {
     int32_t cycles_per_graph; /* cycles captured per CUDA graph launch (0 = default, 16) */
     int32_t seg_len;          /* cells per thread along the sweep axis (0 = automatic) */
     int32_t block_lines;      /* lines (threads) per block (0 = automatic, 128) */
-    int32_t materialize_eos;  /* write p, c, g of the real cells on every pass (1, default) or only
-                                 on the last pass of a cycle (0) */
+    int32_t materialize_eos;  /* write p, c, g of the real cells on every pass (1) or only on the
+                                 last pass of a cycle (0, default): the arrays the time loop leaves
+                                 are the same, since every pass's EOS overwrites the previous one */
     int32_t reserved[3];
 } armon_solver_opts;
 

@@ -69,10 +69,11 @@ EXTRA = [
 
 
 @pytest.mark.parametrize("case", EXTRA, ids=lambda c: f"{c.test}-{c.scheme}-{c.projection}-{c.nx}x{c.ny}")
-@pytest.mark.parametrize("seg_len,graph", [(0, 16), (16, 0), (23, 3)])
-def test_fused_solver_matches_oracle_bitwise(case, seg_len, graph):
+@pytest.mark.parametrize("seg_len,graph,eos_every_pass", [(0, 16, 0), (16, 0, 1), (23, 3, 0)])
+def test_fused_solver_matches_oracle_bitwise(case, seg_len, graph, eos_every_pass):
+    # p, c, g written on every pass or on the last pass of each cycle: the same final arrays
     po, ref = _oracle_fields(case)
-    s, p, status = run_solver(case, seg_len=seg_len, cycles_per_graph=graph)
+    s, p, status = run_solver(case, seg_len=seg_len, cycles_per_graph=graph, materialize_eos=eos_every_pass)
     with s:
         assert status == 0 and p.cycle == po.cycle
         assert p.next_cycle_dt == po.next_cycle_dt and p.time == po.time

@@ -130,6 +130,7 @@ def lib() -> C.CDLL:
     L.armon_solver_conservation.argtypes = [S, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.armon_solver_kernel_launches.argtypes = [S]
     L.armon_solver_kernel_launches.restype = C.c_int64
+    L.armon_solver_tiling.argtypes = [S, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.armon_solve_host.argtypes = [P, C.POINTER(SolverOpts), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), P]
     B = C.c_void_p
     L.armon_batch_opts_default.argtypes = [C.POINTER(BatchOpts)]
@@ -300,6 +301,12 @@ class Solver:
     @property
     def kernel_launches(self) -> int:
         return int(lib().armon_solver_kernel_launches(self._h))
+
+    def tiling(self) -> tuple[tuple[int, int], tuple[int, int]]:
+        """((seg_len X, seg_len Y), (blocks X, blocks Y)) of the fused pass."""
+        sl, nb = (C.c_int32 * 2)(), (C.c_int32 * 2)()
+        check(lib().armon_solver_tiling(self._h, sl, nb))
+        return (sl[0], sl[1]), (nb[0], nb[1])
 
 
 def real_cells(p: Params, a: np.ndarray) -> np.ndarray:

@@ -23,6 +23,12 @@ cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets,
                                int scheme, int proj, bool last, int block, cudaStream_t st);
 
 // Blocks of the batch kernel (last pass of a cycle) resident on one SM.
+int sweep_blocks_per_sm_f64(int scheme, int proj, int block);
+int sweep_blocks_per_sm_f32(int scheme, int proj, int block);
+inline int sweep_blocks_per_sm(bool fp32, int scheme, int proj, int block)
+{
+    return fp32 ? sweep_blocks_per_sm_f32(scheme, proj, block) : sweep_blocks_per_sm_f64(scheme, proj, block);
+}
 int sweep_batch_blocks_per_sm_f64(int scheme, int proj, int block);
 int sweep_batch_blocks_per_sm_f32(int scheme, int proj, int block);
 inline int sweep_batch_blocks_per_sm(bool fp32, int scheme, int proj, int block)

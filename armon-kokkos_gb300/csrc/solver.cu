@@ -7,9 +7,12 @@
 // after each batch the host reads the 48-byte state back to test the reference's loop condition
 // (time < max_time && cycle < max_cycles).  Cycles issued past the end are no-ops on the device.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -44,6 +47,9 @@ struct armon_solver {
     int graph_cycles = 0;
     int64_t launches = 0;
     bool begun = false;
+    int64_t partials_cap = 0;       // blocks the dt partials have room for
+    int tuned_seg[2] = {0, 0};      // measured segment lengths per axis (0: the model's)
+    bool tuned = false;
 };
 
 namespace {
@@ -66,7 +72,8 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
     T* const* arr = reinterpret_cast<T* const*>(s->arr);
     // set 0: rho umat vmat Emat; set 1: the four work arrays (free in the fused path)
     DomainBuffers<T> b{{{arr[2], arr[3], arr[4], arr[5]}, {arr[11], arr[12], arr[13], arr[14]}}, arr[6], arr[7], arr[8]};
-    const int forced[2] = {s->o.seg_len, s->o.seg_len};
+    const int forced[2] = {s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[0],
+                           s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[1]};
     s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, forced, b, s->d_state, s->d_partials,
                                  s->o.materialize_eos, a);
 }
@@ -127,6 +134,127 @@ int enqueue(armon_solver* s, int n_cycles)
         }
     }
     return enqueue_direct(s, n_cycles);
+}
+
+// Tiling of a lone domain, measured.  With the GPU to itself, the best segment length depends on
+// more than the cells a thread walks (how full the last wave of blocks is, how many blocks share an
+// SM, cache traffic), so before the first cycle the solver times the pass of cycle 0 -- which reads
+// one buffer set, writes the other and leaves the step state alone -- with a few candidate tilings
+// (the model's, and segments aiming at 1, 2, 3, 4, 6 and 8 waves of resident blocks), keeps the
+// fastest for both axes and caches it per geometry for the process.  Results never depend on the
+// tiling.  Domains under 2^20 cells, single-pass splittings and a caller-fixed seg_len are left to
+// the model.
+std::map<std::array<int, 7>, std::array<int, 2>> g_tilings;
+std::mutex g_tilings_mu;
+
+int launch_pass0(armon_solver* s)
+{
+    cudaError_t e;
+    if (s->fp32) {
+        s->a32.pass = 0;
+        e = launch_sweep(s->a32, s->p.scheme, s->p.projection, false, s->grid, s->block, s->stream);
+    } else {
+        s->a64.pass = 0;
+        e = launch_sweep(s->a64, s->p.scheme, s->p.projection, false, s->grid, s->block, s->stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+    s->launches++;
+    return ARMON_OK;
+}
+
+void refill(armon_solver* s)
+{
+    if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+}
+
+int ensure_partials(armon_solver* s)
+{
+    if (s->grid <= s->partials_cap) return ARMON_OK;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    CUDA_TRY(cudaFree(s->d_partials));
+    s->d_partials = nullptr;
+    CUDA_TRY(cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)s->grid));
+    s->partials_cap = s->grid;
+    if (s->fp32) s->a32.partials = s->d_partials; else s->a64.partials = s->d_partials;
+    return ARMON_OK;
+}
+
+int tune_tiling(armon_solver* s)
+{
+    if (s->tuned || s->o.seg_len > 0 || s->npass < 2) return ARMON_OK;
+    s->tuned = true;
+    const armon_params& p = s->p;
+    if ((int64_t)p.nx * p.ny < (1 << 20)) return ARMON_OK;
+    const std::array<int, 7> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting, s->block};
+    {
+        std::lock_guard<std::mutex> lk(g_tilings_mu);
+        auto it = g_tilings.find(key);
+        if (it != g_tilings.end()) {
+            s->tuned_seg[0] = it->second[0];
+            s->tuned_seg[1] = it->second[1];
+            refill(s);
+            return ensure_partials(s);
+        }
+    }
+    const StepState& st = *s->h_state;
+    if (!(st.status == STATUS_RUNNING && st.time < p.max_time && st.cycle < p.max_cycles)) return ARMON_OK;
+
+    // candidates: the model's tiling, then segments aiming at w waves of resident blocks per axis
+    const int slots = s->sm_count * sweep_blocks_per_sm(s->fp32, p.scheme, p.projection, s->block);
+    const int halo = stencil_reach(&p);
+    std::vector<std::array<int, 2>> cand;
+    std::array<int, 2> model;
+    for (int axis = 0; axis < 2; axis++) {
+        const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
+        model[axis] = choose_segments(n, nl, s->block, halo, s->sm_count, 0).seg_len;
+    }
+    cand.push_back(model);
+    for (int w : {1, 2, 3, 4, 6, 8}) {
+        std::array<int, 2> c;
+        for (int axis = 0; axis < 2; axis++) {
+            const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
+            const AxisTiling t = axis_tiling(n, nl, s->block, n);   // one segment: nlb, spb
+            const int per_line = std::max(1, (int)std::lround(double(w) * slots * t.spb / t.nlb));
+            c[axis] = std::max(16, (n + per_line - 1) / per_line);
+        }
+        if (std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+    }
+
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    std::array<int, 2> best = model;
+    int rc = ARMON_OK;
+    for (const auto& c : cand) {
+        s->tuned_seg[0] = c[0];
+        s->tuned_seg[1] = c[1];
+        refill(s);
+        rc = launch_pass0(s);                                    // warm-up
+        if (rc == ARMON_OK && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        for (int k = 0; k < 2 && rc == ARMON_OK; k++) rc = launch_pass0(s);
+        if (rc == ARMON_OK && cudaEventRecord(e1, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        float ms = 0;
+        if (rc == ARMON_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc != ARMON_OK) break;
+        if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != ARMON_OK) { set_error("tiling measurement failed"); return rc; }
+    s->tuned_seg[0] = best[0];
+    s->tuned_seg[1] = best[1];
+    refill(s);
+    {
+        std::lock_guard<std::mutex> lk(g_tilings_mu);
+        g_tilings[key] = best;
+    }
+    return ensure_partials(s);
 }
 
 // Puts the current state back into set 0 (rho, umat, vmat, Emat) so that the reference's
@@ -211,6 +339,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     int pblocks = std::max(s->grid, s->sm_count * 8);
     s->cons_grid = s->sm_count * 4;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)pblocks);
+    s->partials_cap = pblocks;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_cons, sizeof(double) * (2 * (size_t)s->cons_grid + 2));
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
@@ -274,7 +403,9 @@ int armon_solver_begin_loop(armon_solver* s)
     CUDA_TRY(launch_begin(b, s->fp32, s->sm_count * 4, s->stream));
     s->launches++;
     s->begun = true;
-    return sync_state(s);
+    int rc = sync_state(s);
+    if (rc == ARMON_OK) rc = tune_tiling(s);
+    return rc;
 }
 
 int armon_solver_init_test(armon_solver* s)
@@ -428,6 +559,17 @@ int armon_solver_conservation(armon_solver* s, double* mass, double* energy)
 }
 
 int64_t armon_solver_kernel_launches(armon_solver* s) { return s->launches; }
+
+int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2])
+{
+    for (int axis = 0; axis < 2; axis++) {
+        const int sl = s->fp32 ? s->a32.geom[axis].seg_len : s->a64.geom[axis].seg_len;
+        const int nb = s->fp32 ? s->a32.geom[axis].blocks : s->a64.geom[axis].blocks;
+        if (seg_len) seg_len[axis] = sl;
+        if (blocks) blocks[axis] = nb;
+    }
+    return ARMON_OK;
+}
 
 int armon_solve_host(const armon_params* p, const armon_solver_opts* opts, const double* const in[4],
                      double* const out[5], armon_params* final_state)

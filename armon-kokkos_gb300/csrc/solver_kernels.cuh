@@ -186,6 +186,21 @@ static cudaError_t launch_sweep_batch_t(const SweepArgs<T>* doms, const int* off
 #undef ARMON_B
 }
 
+// Blocks of the (heavier) last-pass single-domain kernel that fit on one SM.
+template <class T>
+static int sweep_blocks_per_sm_t(int scheme, int proj, int block)
+{
+    int n = 0;
+    cudaError_t e;
+    if (scheme == 1)
+        e = proj == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_kernel<T, 1, 2, true>, block, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_kernel<T, 1, 1, true>, block, 0);
+    else
+        e = proj == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_kernel<T, 0, 2, true>, block, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_kernel<T, 0, 1, true>, block, 0);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
 // Blocks of the (heavier) last-pass batch kernel that fit on one SM.
 template <class T>
 static int sweep_batch_blocks_per_sm_t(int scheme, int proj, int block)

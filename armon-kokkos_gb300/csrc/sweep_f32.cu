@@ -19,6 +19,11 @@ cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets,
     return launch_sweep_batch_t<float>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
 }
 
+int sweep_blocks_per_sm_f32(int scheme, int proj, int block)
+{
+    return sweep_blocks_per_sm_t<float>(scheme, proj, block);
+}
+
 int sweep_batch_blocks_per_sm_f32(int scheme, int proj, int block)
 {
     return sweep_batch_blocks_per_sm_t<float>(scheme, proj, block);

@@ -17,6 +17,11 @@ cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets
     return launch_sweep_batch_t<double>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
 }
 
+int sweep_blocks_per_sm_f64(int scheme, int proj, int block)
+{
+    return sweep_blocks_per_sm_t<double>(scheme, proj, block);
+}
+
 int sweep_batch_blocks_per_sm_f64(int scheme, int proj, int block)
 {
     return sweep_batch_blocks_per_sm_t<double>(scheme, proj, block);

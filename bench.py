@@ -241,7 +241,7 @@ def run_gpu(args) -> None:
     # a dedicated stream: the solver launches on it and the CUDA events are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len)
     s.init_test()
     s.enqueue_cycles(W)
     torch.cuda.synchronize()
@@ -253,6 +253,7 @@ def run_gpu(args) -> None:
 
     barrier()
     launches0 = s.kernel_launches
+    tiling = s.tiling()
     sampler = ClockSampler() if rank == 0 else None
     if sampler:
         sampler.start()
@@ -282,7 +283,8 @@ def run_gpu(args) -> None:
     case_e2e = A.Case(**WORKLOAD)
     case_e2e.nx, case_e2e.ny = nx, ny
     case_e2e.max_cycles = K
-    se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph)
+    se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
+                  seg_len=args.seg_len)
     se.init_test()
     outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
             for k in ("rho", "umat", "vmat", "Emat", "pmat")}
@@ -314,7 +316,8 @@ def run_gpu(args) -> None:
         tr = profiled_traffic()
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64" if prec == 64 else "f32", "data": "synthetic", "config": config(nx, ny, world, prec),
+               "dtype": "f64" if prec == 64 else "f32", "data": "synthetic",
+               "config": dict(config(nx, ny, world, prec), seg_len=list(tiling[0]), blocks=list(tiling[1])),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_source": peak_kind,
                             "traffic": (tr * cells if (tr and prec == 64) else None),
@@ -468,6 +471,7 @@ def main():
     ap.add_argument("--size", type=int, default=0, help="cells per side (default 4096; 8192 for --precision 32)")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
+    ap.add_argument("--seg-len", type=int, default=0, help="cells per thread along the sweep axis (0 = automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],

@@ -140,6 +140,12 @@ int armon_solver_conservation(armon_solver* s, double* mass, double* energy);
 /* Number of kernels the solver launched so far (diagnostics). */
 int64_t armon_solver_kernel_launches(armon_solver* s);
 
+/* The tiling of the fused pass per axis (X, Y): cells per thread along the axis and blocks per
+ * launch.  Unless opts.seg_len fixes it, a domain of 2^20 cells or more gets the fastest of a few
+ * candidate tilings, timed on its cycle-0 pass at the start of its first time loop (no change to
+ * the state or the results); smaller domains use the cost model. */
+int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2]);
+
 /* ---- batches: many independent domains advanced together (no counterpart in the reference;
  *      each domain follows time_loop, src/armon_2D.cpp:327-386, on its own) ---- */
 typedef struct armon_batch armon_batch;

@@ -171,3 +171,24 @@ def test_invalid_dt_is_reported_not_fatal():
         assert ei.value.code == A.ERR_INVALID_DT
         _, status = s.state()
         assert status == 1
+
+
+def test_measured_tiling_keeps_results():
+    # a domain large enough for the solver to time its candidate tilings on the cycle-0 pass;
+    # whatever it picks, the cycles give the same bits as fixed tilings
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=1024, ny=1024, cfl=0.6,
+                  max_cycles=4, max_time=1e9, test_option=0.04)
+    out = []
+    for seg in (0, 64, 1024):
+        s, p, status = run_solver(case, seg_len=seg)
+        with s:
+            assert status == 0 and p.cycle == 4
+            (sx, sy), (bx, by) = s.tiling()
+            assert sx > 0 and sy > 0 and bx > 0 and by > 0
+            if seg:
+                assert (sx, sy) == (seg, seg)
+            out.append({k: s.download(k) for k in FIELDS})
+    for other in out[1:]:
+        for k in FIELDS:
+            assert np.array_equal(out[0][k].view(np.int64), other[k].view(np.int64)), k
+

@@ -55,9 +55,10 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profiled(key: str) -> float | None:
-    """A per-cell figure from the committed ncu summary (profiles/sweep_f64_sod_circ.md)."""
-    path = os.path.join(ROOT, "profiles", "sweep_f64_sod_circ.md")
+def profiled(key: str, precision: int = 64) -> float | None:
+    """A per-cell figure from the committed ncu summary (profiles/sweep_f64_sod_circ.md or
+    profiles/sweep_f32_sod_circ.md)."""
+    path = os.path.join(ROOT, "profiles", "sweep_f%d_sod_circ.md" % precision)
     try:
         txt = open(path).read()
     except OSError:
@@ -66,9 +67,9 @@ def profiled(key: str) -> float | None:
     return float(m.group(1)) if m else None
 
 
-def profiled_traffic() -> float | None:
+def profiled_traffic(precision: int = 64) -> float | None:
     """DRAM bytes per cell and sweep launch (scaled to the workload by the caller)."""
-    return profiled("traffic_bytes_per_cell_per_pass")
+    return profiled("traffic_bytes_per_cell_per_pass", precision)
 
 
 class ClockSampler:
@@ -313,18 +314,20 @@ def run_gpu(args) -> None:
         t_launch = ms_max / 1e3 / (K * 2)
         bpc = BYTES_PER_CELL_UPDATE if prec == 64 else BYTES_PER_CELL_UPDATE // 2
         achieved = bpc / 2 * cells / t_launch / 1e9
-        tr = profiled_traffic()
+        tr = profiled_traffic(prec)
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64" if prec == 64 else "f32", "data": "synthetic",
                "config": dict(config(nx, ny, world, prec), seg_len=list(tiling[0]), blocks=list(tiling[1])),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_source": peak_kind,
-                            "traffic": (tr * cells if (tr and prec == 64) else None),
+                            "traffic": (tr * cells if tr else None),
                             "kernel": "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)"
                                       % ("double" if prec == 64 else "float"),
                             "algorithmic_bytes_per_launch": bpc / 2 * cells,
-                            "note": "not HBM-bound: the FP64 pipe and integer latency bound the pass (fp64_roofline, profiles/)"},
+                            "note": ("not HBM-bound: the FP64 pipe and integer latency bound the pass (fp64_roofline, profiles/)"
+                                     if prec == 64 else
+                                     "not HBM-bound: instruction latency bounds the pass (12 warps per SM; profiles/)")},
                "fp64_roofline": fp64_roofline(cells, ms_max / 1e3 / K, clocks) if prec == 64 else None,
                "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
                        "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,

@@ -145,6 +145,21 @@ def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None) -> dict |
                     "additions and multiplications count here"}
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest of every rank's x (the slowest rank's time); the identity on one rank."""
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Units all ranks processed (each rank a replica of the same workload) over the slowest time."""
+    return units_per_rank * world / seconds_max
+
+
 def dist_info() -> tuple[int, int, int]:
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -270,12 +285,9 @@ def run_gpu(args) -> None:
     p, status = s.state()
     if status != 0 or p.cycle != W + K:
         raise RuntimeError(f"solver state after the timed region: status {status}, cycle {p.cycle}")
-    ms_t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = max_over_ranks(ms, world)
     cells = nx * ny
-    value = cells * K * world / (ms_max / 1e3)
+    value = whole_job_rate(cells * K, world, ms_max / 1e3)
 
     # end to end through the C ABI with host buffers: H2D of the initial fields from pinned memory,
     # the time loop, D2H of rho, u, v, E, p (every step of it inside the timed region)
@@ -304,10 +316,7 @@ def run_gpu(args) -> None:
     assert st_e == 0 and pe.cycle == K
     se.close()
     nb = se.params.nb_cells if hasattr(se, "params") else (nx + 10) * (ny + 10)
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = cells * K * world / float(e2e_t.item())
+    e2e_value = whole_job_rate(cells * K, world, max_over_ranks(e2e_s, world))
 
     if rank == 0:
         peak, peak_kind = measured_peaks()

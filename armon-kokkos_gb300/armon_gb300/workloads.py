@@ -38,10 +38,12 @@ class DomainSpec:
     p_r: float
     t_end: float = 0.15
     precision: int = 64
+    splitting: str = "Sequential"
 
     def case(self) -> Case:
         return Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", limiter="Minmod", nghost=5,
-                    nx=self.nx, ny=self.ny, cfl=0.6, max_time=self.t_end, max_cycles=1_000_000)
+                    nx=self.nx, ny=self.ny, cfl=0.6, max_time=self.t_end, max_cycles=1_000_000,
+                    splitting=self.splitting)
 
     def params(self) -> Params:
         return make_params(self.case())

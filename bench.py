@@ -145,6 +145,34 @@ def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None) -> dict |
                     "additions and multiplications count here"}
 
 
+def l1_rel(a, b) -> float:
+    """sum |a - b| / sum |b| (b the FP64 result)."""
+    import numpy as np
+
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def fp32_accuracy(A, case, graph: int) -> dict:
+    """The FP32 variant against the FP64 solve of the same case and cycles (the FP64 solver is
+    bit-identical to the FP64 oracle): L1 relative error of rho and E, and the relative drift of the
+    mass and energy sums (FP64 sums in both) over the run."""
+    res = {}
+    for prec in (64, 32):
+        with A.Solver(case, precision=prec, cycles_per_graph=graph) as s:
+            s.init_test()
+            m0, e0 = s.conservation()
+            s.run()
+            p, status = s.state()
+            m1, e1 = s.conservation()
+            res[prec] = ({k: A.real_cells(s.params, s.download(k)) for k in ("rho", "Emat")},
+                         (m1 - m0) / m0, (e1 - e0) / e0, p.cycle, status)
+    f64, f32 = res[64], res[32]
+    return {"cycles": f32[3], "l1_rho": l1_rel(f32[0]["rho"], f64[0]["rho"]),
+            "l1_E": l1_rel(f32[0]["Emat"], f64[0]["Emat"]),
+            "mass_drift": {"f32": f32[1], "f64": f64[1]}, "energy_drift": {"f32": f32[2], "f64": f64[2]},
+            "against": "the FP64 solve of the same workload and cycles (bit-identical to the FP64 oracle)"}
+
+
 def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
     """The largest of every rank's x (the slowest rank's time); the identity on one rank."""
     import torch
@@ -345,6 +373,11 @@ def run_gpu(args) -> None:
                "gpu_launches": launches, "clocks": clocks}
         if world == 1 and not args.no_cpu and prec == 64:
             out["cpu_baseline"] = cpu_port_throughput(nx, ny, args.cpu_seconds, 200)
+        if world == 1 and prec == 32 and args.accuracy_cycles > 0:
+            acc_case = A.Case(**WORKLOAD)
+            acc_case.nx, acc_case.ny = nx, ny
+            acc_case.max_cycles = args.accuracy_cycles
+            out["accuracy"] = fp32_accuracy(A, acc_case, args.graph)
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -458,10 +491,26 @@ def run_serve(args) -> None:
         s_, w_ = plain_solve(A, r.spec, r.spec.precision, args.graph)
         p_secs += s_
         p_work += w_
+    # FP32 requests against the same solve in FP64 (served results equal solo ones bit for bit)
+    l1 = []
+    for r in [r for r in trace if r.spec.precision == 32][:args.accuracy_sample]:
+        fields = {}
+        for prec in (64, 32):
+            with A.Solver(r.spec.params(), precision=prec) as s:
+                s.init_test()
+                for k, a in r.spec.initial_state().items():
+                    s.upload(k, a)
+                s.begin_loop()
+                s.run()
+                fields[prec] = {k: A.real_cells(s.params, s.download(k)) for k in ("rho", "Emat")}
+        l1.append((l1_rel(fields[32]["rho"], fields[64]["rho"]), l1_rel(fields[32]["Emat"], fields[64]["Emat"])))
     value = work / wall
     out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 1, "warmup": 1,
            "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64+f32", "data": "synthetic",
+           "fp32_accuracy": {"requests": len(l1), "l1_rho_max": max((a for a, _ in l1), default=None),
+                             "l1_E_max": max((b for _, b in l1), default=None),
+                             "against": "each request solved alone in FP64 (to its own t_end; cycle counts may differ)"},
            "config": {"workload": f"{len(trace)} requests, Poisson arrivals at {args.rate}/s (seed 7), side "
                                   "lognormal(6, 0.6) clipped to [128, 2048], FP64 or FP32 (p = 1/2), t_end ~ U(0.05, 0.2), "
                                   "150 GB state budget",
@@ -486,6 +535,8 @@ def main():
     ap.add_argument("--seg-len", type=int, default=0, help="cells per thread along the sweep axis (0 = automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--accuracy-cycles", type=int, default=100,
+                    help="--precision 32: cycles of the FP32-vs-FP64 accuracy run (0 = skip)")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
                     help="single: the 4096^2 drop-in case (default); batch: 256 mixed domains; serve: a request trace")
     ap.add_argument("--domains", type=int, default=256, help="--workload batch: domains")
@@ -493,6 +544,7 @@ def main():
     ap.add_argument("--rate", type=float, default=50.0, help="--workload serve: arrivals per second")
     ap.add_argument("--serve-cycles", type=int, default=8, help="--workload serve: cycles per round")
     ap.add_argument("--plain-sample", type=int, default=100, help="--workload serve: requests timed on the plain path")
+    ap.add_argument("--accuracy-sample", type=int, default=5, help="--workload serve: FP32 requests checked against FP64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -43,6 +44,7 @@ struct armon_server {
     Clock::time_point t0;
     std::map<BatchKey, armon_batch*> batches;
     std::map<armon_batch*, bool> busy;  // cycles enqueued and not yet collected
+    std::map<BatchKey, int64_t> inflight_cells;   // real cells of the running solves per batch
     std::vector<Request> reqs;
     std::deque<int64_t> queue;        // waiting, in submission order
     std::vector<int64_t> running;     // on the device, loop not ended
@@ -57,9 +59,14 @@ double now(const armon_server* s)
     return std::chrono::duration<double>(Clock::now() - s->t0).count();
 }
 
+BatchKey key_of(const armon_params& p, int32_t precision)
+{
+    return BatchKey{precision, p.scheme, p.projection, p.axis_splitting};
+}
+
 int batch_for(armon_server* s, const armon_params& p, int32_t precision, armon_batch** out)
 {
-    BatchKey key{precision, p.scheme, p.projection, p.axis_splitting};
+    BatchKey key = key_of(p, precision);
     auto it = s->batches.find(key);
     if (it != s->batches.end()) {
         *out = it->second;
@@ -85,12 +92,24 @@ int lookup(armon_server* s, int64_t req, Request** r)
     return ARMON_OK;
 }
 
-// Admits waiting requests in order while the budget allows.
+// Admits waiting requests in order while the memory budget allows.  A request whose batch is at
+// its cell limit stays (and so do the later requests for that batch); requests for other batches
+// may pass it.  The memory budget stops admission at the first request that does not fit.
 int admit(armon_server* s)
 {
-    while (!s->queue.empty()) {
-        const int64_t id = s->queue.front();
+    std::set<BatchKey> full;
+    for (auto it = s->queue.begin(); it != s->queue.end();) {
+        const int64_t id = *it;
         Request& r = s->reqs[(size_t)id];
+        const BatchKey key = key_of(r.p, r.info.precision);
+        if (full.count(key)) { ++it; continue; }
+        const int64_t cells = (int64_t)r.p.nx * r.p.ny;
+        int64_t& inflight = s->inflight_cells[key];
+        if (s->o.max_inflight_cells > 0 && inflight > 0 && inflight + cells > s->o.max_inflight_cells) {
+            full.insert(key);
+            ++it;
+            continue;
+        }
         const int64_t need = armon_batch_domain_bytes(&r.p, r.info.precision);
         if (s->o.memory_budget > 0 && s->bytes + need > s->o.memory_budget) break;
         armon_batch* b = nullptr;
@@ -99,7 +118,7 @@ int admit(armon_server* s)
         int32_t dom = -1;
         rc = r.has_sod ? armon_batch_add_sod(b, &r.p, &r.sod, &dom) : armon_batch_add(b, &r.p, nullptr, &dom);
         if (rc == ARMON_ERR_NOMEM) break;          // the device is full after all: retry next round
-        s->queue.pop_front();
+        it = s->queue.erase(it);
         if (rc != ARMON_OK) {                      // this request cannot run: report it as failed
             r.info.status = ARMON_REQ_FAILED;
             r.info.t_done = now(s);
@@ -112,6 +131,7 @@ int admit(armon_server* s)
         r.info.bytes = need;
         r.info.t_admit = now(s);
         s->bytes += need;
+        inflight += cells;
         s->running.push_back(id);
     }
     return ARMON_OK;
@@ -217,6 +237,7 @@ int armon_server_step(armon_server* s, int32_t* in_flight, int32_t* queued)
         int32_t status = 0;
         armon_batch_domain_state(r.batch, r.dom, &fp, &status);
         r.info.status = status == 0 ? ARMON_REQ_DONE : ARMON_REQ_FAILED;
+        s->inflight_cells[key_of(r.p, r.info.precision)] -= (int64_t)r.p.nx * r.p.ny;
         r.info.cycle = fp.cycle;
         r.info.time = fp.time;
         r.info.t_done = t;

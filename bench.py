@@ -471,7 +471,8 @@ def run_serve(args) -> None:
     # warm-up: the kernels of both precisions
     with A.Server(cycles_per_step=args.serve_cycles) as srv:
         S.replay(srv, W.serving_trace(n=4, rate=1000.0, seed=1, side_range=(128, 128)))
-    with A.Server(memory_budget=150_000_000_000, cycles_per_step=args.serve_cycles) as srv:
+    with A.Server(memory_budget=150_000_000_000, cycles_per_step=args.serve_cycles,
+                  max_inflight_cells=args.max_inflight) as srv:
         sampler = ClockSampler()
         sampler.start()
         served, wall = S.replay(srv, trace)
@@ -514,7 +515,8 @@ def run_serve(args) -> None:
            "config": {"workload": f"{len(trace)} requests, Poisson arrivals at {args.rate}/s (seed 7), side "
                                   "lognormal(6, 0.6) clipped to [128, 2048], FP64 or FP32 (p = 1/2), t_end ~ U(0.05, 0.2), "
                                   "150 GB state budget",
-                      "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work},
+                      "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work,
+                      "max_inflight_cells": args.max_inflight},
            "tts_p50_s": S.percentile(tts, 0.5), "tts_p99_s": S.percentile(tts, 0.99), "by_precision": by_prec,
            "plain": {"value": p_work / p_secs, "seconds": p_secs, "sample": f"the first {len(sample)} requests",
                      "path": "one Solver per request, one after another (time loops only)"},
@@ -545,6 +547,8 @@ def main():
     ap.add_argument("--serve-cycles", type=int, default=8, help="--workload serve: cycles per round")
     ap.add_argument("--plain-sample", type=int, default=100, help="--workload serve: requests timed on the plain path")
     ap.add_argument("--accuracy-sample", type=int, default=5, help="--workload serve: FP32 requests checked against FP64")
+    ap.add_argument("--max-inflight", type=int, default=None,
+                    help="--workload serve: real cells running at once per batch (0 = no limit; default: the server's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

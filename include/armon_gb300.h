@@ -232,7 +232,9 @@ int64_t armon_batch_kernel_launches(armon_batch* b);
 
 /* ---- serving: a request loop over batches (no counterpart in the reference) ----
  * Solves are submitted as requests and wait in a first-come-first-served queue.  Each round
- * admits waiting requests while their state fits in the memory budget, then advances every
+ * admits waiting requests while their state fits in the memory budget (and their batch is under
+ * its cell limit: a request whose batch is full waits, without holding back requests for other
+ * batches, and is never overtaken by a later request for the same batch), then advances every
  * admitted solve by a few cycles: solves of one precision and scheme share a batch (one fused
  * launch per pass for all of them), different batches run on their own streams and overlap on the
  * device.  A solve's state stays on the device from admission until the caller releases it;
@@ -244,7 +246,10 @@ typedef struct armon_server_opts {
     int64_t memory_budget;     /* device bytes of solve state held at once (default 150e9) */
     int32_t cycles_per_step;   /* cycles of every running solve per round (default 8) */
     int32_t block_lines;       /* as armon_batch_opts (default 128) */
-    int32_t reserved[4];
+    int64_t max_inflight_cells;/* real cells running at once in one batch (0 = no limit): beyond
+                                  what saturates the GPU, more solves at once only share it, and
+                                  every one of them finishes later */
+    int32_t reserved[2];
 } armon_server_opts;
 
 enum { ARMON_REQ_QUEUED = 0, ARMON_REQ_RUNNING = 1, ARMON_REQ_DONE = 2, ARMON_REQ_FAILED = 3 };

@@ -97,3 +97,29 @@ def test_unsupported_request_fails_alone():
                 break
         assert done[bad] == A.REQ_FAILED
         assert all(done[g] == A.REQ_DONE for g in good)
+
+
+def test_cell_limit_keeps_batches_under_it_in_order():
+    specs = W.mixed_domains(10, seed=12, sides=(32, 48, 64))
+    for k, s in enumerate(specs):
+        s.t_end = 0.03
+        s.precision = 64 if k % 2 == 0 else 32
+    cap = 2 * 64 * 64
+    with A.Server(cycles_per_step=2, max_inflight_cells=cap) as srv:
+        ids = [srv.submit(s.params(), s.precision, s.sod_interface()) for s in specs]
+        for _ in range(10_000):
+            running, queued = srv.step()
+            for prec in (64, 32):
+                run = [i for i in ids if srv.info(i).status == A.REQ_RUNNING and srv.info(i).precision == prec]
+                cells = sum(srv.info(i).nx * srv.info(i).ny for i in run)
+                assert cells <= cap or len(run) == 1
+            while (r := srv.next_done()) is not None:
+                srv.release(r)
+            if running == 0 and queued == 0:
+                break
+        infos = [srv.info(i) for i in ids]
+        assert all(i.status == A.REQ_DONE for i in infos)
+        for prec in (64, 32):
+            admits = [i.t_admit for i in infos if i.precision == prec]
+            assert admits == sorted(admits)            # first come, first served within a batch
+

@@ -50,6 +50,7 @@ struct armon_solver {
     int64_t partials_cap = 0;       // blocks the dt partials have room for
     int tuned_seg[2] = {0, 0};      // measured segment lengths per axis (0: the model's)
     bool tuned = false;
+    double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
 };
 
 namespace {
@@ -134,6 +135,32 @@ int enqueue(armon_solver* s, int n_cycles)
         }
     }
     return enqueue_direct(s, n_cycles);
+}
+
+// FP64 <-> FP32 conversion of a staged array on the device (round to nearest, as the host's cast;
+// widening is exact).
+__global__ void narrow_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+
+__global__ void widen_kernel(const float* __restrict__ in, double* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+int ensure_stage(armon_solver* s)
+{
+    if (s->stage) return ARMON_OK;
+    cudaError_t e = cudaMalloc(&s->stage, (size_t)s->p.nb_cells * sizeof(double));
+    if (e != cudaSuccess) {
+        s->stage = nullptr;
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return ARMON_ERR_NOMEM;
+    }
+    return ARMON_OK;
 }
 
 // Tiling of a lone domain, measured.  With the GPU to itself, the best segment length depends on
@@ -371,6 +398,7 @@ void armon_solver_destroy(armon_solver* s)
     if (s->h_state) cudaFreeHost(s->h_state);
     if (s->d_partials) cudaFree(s->d_partials);
     if (s->d_cons) cudaFree(s->d_cons);
+    if (s->stage) cudaFree(s->stage);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -495,10 +523,13 @@ int armon_solver_download(armon_solver* s, int which, double* host)
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         return ARMON_OK;
     }
-    std::vector<float> tmp(n);
-    CUDA_TRY(cudaMemcpyAsync(tmp.data(), s->arr[k], n * 4, cudaMemcpyDeviceToHost, s->stream));
+    rc = ensure_stage(s);
+    if (rc != ARMON_OK) return rc;
+    widen_kernel<<<s->sm_count * 8, 256, 0, s->stream>>>((const float*)s->arr[k], s->stage, (int64_t)n);
+    CUDA_TRY(cudaGetLastError());
+    s->launches++;
+    CUDA_TRY(cudaMemcpyAsync(host, s->stage, n * 8, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (size_t i = 0; i < n; i++) host[i] = tmp[i];
     return ARMON_OK;
 }
 
@@ -514,9 +545,12 @@ int armon_solver_upload(armon_solver* s, int which, const double* host)
         CUDA_TRY(cudaStreamSynchronize(s->stream));
         return ARMON_OK;
     }
-    std::vector<float> tmp(n);
-    for (size_t i = 0; i < n; i++) tmp[i] = (float)host[i];
-    CUDA_TRY(cudaMemcpyAsync(s->arr[k], tmp.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
+    rc = ensure_stage(s);
+    if (rc != ARMON_OK) return rc;
+    CUDA_TRY(cudaMemcpyAsync(s->stage, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+    narrow_kernel<<<s->sm_count * 8, 256, 0, s->stream>>>(s->stage, (float*)s->arr[k], (int64_t)n);
+    CUDA_TRY(cudaGetLastError());
+    s->launches++;
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     return ARMON_OK;
 }

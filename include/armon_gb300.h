@@ -128,7 +128,8 @@ int armon_solver_sync_params(armon_solver* s, armon_params* p, int32_t* status);
 
 /* Host <-> device copies of whole arrays (nb_cells values each, in the reference's layout).
  * `which` names an array: 0 x, 1 y, 2 rho, 3 umat, 4 vmat, 5 Emat, 6 pmat, 7 cmat, 8 gmat,
- * 9 ustar, 10 pstar, 11..14 work arrays, 15 domain_mask.  FP32 solvers convert. */
+ * 9 ustar, 10 pstar, 11..14 work arrays, 15 domain_mask.  FP32 solvers convert on the device,
+ * through an FP64 staging array of nb_cells values allocated on the first such call. */
 int armon_solver_download(armon_solver* s, int which, double* host);
 int armon_solver_upload(armon_solver* s, int which, const double* host);
 /* Device pointer of an FP64 array (NULL for an FP32 solver) */

@@ -518,9 +518,9 @@ def run_serve(args) -> None:
                       "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work,
                       "max_inflight_cells": args.max_inflight},
            "tts_p50_s": S.percentile(tts, 0.5), "tts_p99_s": S.percentile(tts, 0.99), "by_precision": by_prec,
-           "plain": {"value": p_work / p_secs, "seconds": p_secs, "sample": f"the first {len(sample)} requests",
-                     "path": "one Solver per request, one after another (time loops only)"},
-           "served_over_plain": value / (p_work / p_secs),
+           "plain": ({"value": p_work / p_secs, "seconds": p_secs, "sample": f"the first {len(sample)} requests",
+                      "path": "one Solver per request, one after another (time loops only)"} if sample else None),
+           "served_over_plain": value / (p_work / p_secs) if sample else None,
            "gpu_launches": launches, "clocks": clocks}
     print(json.dumps(out), flush=True)
 

@@ -105,6 +105,20 @@ int cuda_fail(cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail(e_, #expr);       \
     } while (0)
 
+// FP64 <-> FP32 conversion of staged arrays on the device (round to nearest, as the host's cast;
+// widening is exact); the staging array comes from the batch's pool for the one transfer.
+__global__ void narrow_kernel(const double* __restrict__ in, float* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+
+__global__ void widen_kernel(const float* __restrict__ in, double* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
 template <class T>
 DomainBuffers<T> buffers(const Dom& d)
 {
@@ -506,9 +520,15 @@ int add_domain(armon_batch* b, const armon_params* p, const double* const init[4
             if (!b->fp32) {
                 CUDA_TRY(cudaMemcpyAsync(dd.arr[k], init[k], (size_t)p->nb_cells * 8, cudaMemcpyHostToDevice, b->stream));
             } else {
-                std::vector<float> f(init[k], init[k] + p->nb_cells);
-                CUDA_TRY(cudaMemcpyAsync(dd.arr[k], f.data(), (size_t)p->nb_cells * 4, cudaMemcpyHostToDevice, b->stream));
-                CUDA_TRY(cudaStreamSynchronize(b->stream));
+                void* stage = nullptr;
+                CUDA_TRY(cudaMallocFromPoolAsync(&stage, (size_t)p->nb_cells * 8, b->pool, b->stream));
+                CUDA_TRY(cudaMemcpyAsync(stage, init[k], (size_t)p->nb_cells * 8, cudaMemcpyHostToDevice, b->stream));
+                narrow_kernel<<<b->sm_count * 8, 256, 0, b->stream>>>((const double*)stage, (float*)dd.arr[k],
+                                                                      (int64_t)p->nb_cells);
+                CUDA_TRY(cudaGetLastError());
+                b->launches++;
+                CUDA_TRY(cudaFreeAsync(stage, b->stream));
+                CUDA_TRY(cudaStreamSynchronize(b->stream));   // the caller's host array may go away
             }
         }
     }
@@ -637,10 +657,14 @@ int armon_batch_download(armon_batch* b, int32_t id, int which, double* host)
         CUDA_TRY(cudaStreamSynchronize(b->stream));
         return ARMON_OK;
     }
-    std::vector<float> tmp(n);
-    CUDA_TRY(cudaMemcpyAsync(tmp.data(), d.arr[k], n * 4, cudaMemcpyDeviceToHost, b->stream));
+    void* stage = nullptr;
+    CUDA_TRY(cudaMallocFromPoolAsync(&stage, n * 8, b->pool, b->stream));
+    widen_kernel<<<b->sm_count * 8, 256, 0, b->stream>>>((const float*)d.arr[k], (double*)stage, (int64_t)n);
+    CUDA_TRY(cudaGetLastError());
+    b->launches++;
+    CUDA_TRY(cudaMemcpyAsync(host, stage, n * 8, cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaFreeAsync(stage, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
-    for (size_t i = 0; i < n; i++) host[i] = tmp[i];
     return ARMON_OK;
 }
 

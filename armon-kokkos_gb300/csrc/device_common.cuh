@@ -107,13 +107,22 @@ struct DtAcc {
         // kmax of non-negative values: for sign-clear, non-NaN doubles the IEEE order is the
         // unsigned order of the bit patterns, so the compares run on the integer pipes
         const uint64_t inf = 0x7FF0000000000000ull;
-        const uint64_t a1 = sfp::bits(sfp::absval(u + c));
-        const uint64_t a2 = sfp::bits(sfp::absval(u - c));
-        const uint64_t b1 = sfp::bits(sfp::absval(v + c));
-        const uint64_t b2 = sfp::bits(sfp::absval(v - c));
-        // kmax(a1, a2) = (a1 < a2) ? a2 : a1, where a NaN a1 is kept and a NaN a2 is not taken
-        const uint64_t mx = (a1 <= inf && a2 <= inf && a1 < a2) ? a2 : a1;
-        const uint64_t my = (b1 <= inf && b2 <= inf && b1 < b2) ? b2 : b1;
+        uint64_t mx, my;
+        const uint64_t ub = sfp::bits(u), vb = sfp::bits(v), cb = sfp::bits(c);
+        if ((ub & inf) != inf && (vb & inf) != inf && (cb & inf) != inf && (int64_t)cb >= 0) {
+            // finite u, v and c >= +0: max(|u + c|, |u - c|) == RN(|u| + c), since one of the two
+            // is exactly that sum and rounding is monotone (the other's magnitude is smaller)
+            mx = sfp::bits(sfp::absval(u) + c);
+            my = sfp::bits(sfp::absval(v) + c);
+        } else {
+            const uint64_t a1 = sfp::bits(sfp::absval(u + c));
+            const uint64_t a2 = sfp::bits(sfp::absval(u - c));
+            const uint64_t b1 = sfp::bits(sfp::absval(v + c));
+            const uint64_t b2 = sfp::bits(sfp::absval(v - c));
+            // kmax(a1, a2) = (a1 < a2) ? a2 : a1, where a NaN a1 is kept and a NaN a2 is not taken
+            mx = (a1 <= inf && a2 <= inf && a1 < a2) ? a2 : a1;
+            my = (b1 <= inf && b2 <= inf && b1 < b2) ? b2 : b1;
+        }
         if (mx <= inf) {
             const uint64_t cur = sfp::bits(ax);
             if (cur < mx) ax = __longlong_as_double((long long)mx);

@@ -185,6 +185,25 @@ __device__ __forceinline__ T limiter_fn(int L, T r)
     return T(1);
 }
 
+// limiter_fn(L, num / den) for the GAD ratios.  With the minmod limiter, max(0, min(1, num / den))
+// is +0 when num is zero or of the other sign than den, and 1 when |num| >= |den| with the same
+// sign (the rounded quotient is then >= 1), whatever the quotient's rounding; only a ratio inside
+// (0, 1) needs the division.  Zero and non-finite operands take the general path.
+__device__ __forceinline__ double limited_ratio(int L, double num, double den)
+{
+    if (L == 1 && ARMON_SOFT_FP64) {
+        const uint64_t un = sfp::bits(num), ud = sfp::bits(den);
+        const uint64_t an = un & sfp::kAbs, ad = ud & sfp::kAbs;
+        if (an < sfp::kInf && ad < sfp::kInf && ad != 0) {
+            if (an == 0 || ((un ^ ud) >> 63)) return 0.0;
+            if (an >= ad) return 1.0;
+            return qdiv_at<2>(num, den);     // in (0, 1]: min(1, .) and max(0, .) keep it
+        }
+    }
+    return limiter_fn(L, qdiv_at<2>(num, den));
+}
+__device__ __forceinline__ float limited_ratio(int L, float num, float den) { return limiter_fn(L, num / den); }
+
 template <class T>
 __device__ __forceinline__ T slope_minmod(T d_m, T d_p, T r_m, T r_p)
 {
@@ -250,14 +269,10 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, 
     // src/kernels/acoustic.cpp:40-88 for face i (between cells i-s and i), with the differences
     // of faces i-s (Dm1), i (D0), i+s (Dp1):  Gp.us - Cr.ua == Dp1.au, Gc.us - Cl.ua == D0.au,
     // Cl.ua - Gm.us == Dm1.bu, Cr.ua - Gc.us == D0.bu (the same for p).
-    T r_um = qdiv_at<2>(Dp1.au, D0.au + T(1e-6));
-    T r_pm = qdiv_at<2>(Dp1.ap, D0.ap + T(1e-6));
-    T r_up = qdiv_at<2>(Dm1.bu, D0.bu + T(1e-6));
-    T r_pp = qdiv_at<2>(Dm1.bp, D0.bp + T(1e-6));
-    r_um = limiter_fn(L, r_um);
-    r_pm = limiter_fn(L, r_pm);
-    r_up = limiter_fn(L, r_up);
-    r_pp = limiter_fn(L, r_pp);
+    const T r_um = limited_ratio(L, Dp1.au, D0.au + T(1e-6));
+    const T r_pm = limited_ratio(L, Dp1.ap, D0.ap + T(1e-6));
+    const T r_up = limited_ratio(L, Dm1.bu, D0.bu + T(1e-6));
+    const T r_pp = limited_ratio(L, Dm1.bp, D0.bp + T(1e-6));
     T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
     T theta = qhalf(1 - qmul<3>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
@@ -292,6 +307,35 @@ __device__ __forceinline__ Adv<T> lag_diff(const Lag<T>& lo, const Lag<T>& hi)
     return Adv<T>{hi.rho - lo.rho, hi.rua - lo.rua, hi.ruo - lo.ruo, hi.rE - lo.rE};
 }
 
+// When is a face's minmod slope a signed zero fixed by the signs alone?  slope_minmod(d_m, d_p)
+// is +-0 (the sign of d_p) whenever one difference is zero or the two have opposite signs, for any
+// finite positive r_m, r_p; the slope times a finite length factor is then the zero with the sign
+// of d_p XOR the factor's.  These tests decide it on the bit patterns; infinities and NaNs, and
+// quotients that could overflow or underflow to zero, take the general path.
+__device__ __forceinline__ bool slope_is_zero(double d_m, double d_p)
+{
+    const uint64_t um = sfp::bits(d_m), up = sfp::bits(d_p);
+    const uint64_t am = um & sfp::kAbs, ap = up & sfp::kAbs;
+    if (am >= sfp::kInf || ap >= sfp::kInf) return false;
+    return am == 0 || ap == 0 || ((um ^ up) >> 63) != 0;
+}
+
+// num / den is finite for a positive normal den and a finite num whose exponent is not far above
+__device__ __forceinline__ bool quotient_finite(double num, double den)
+{
+    const uint64_t un = sfp::bits(num), ud = sfp::bits(den);
+    const int en = (int)((un >> 52) & 0x7FF), ed = (int)((ud >> 52) & 0x7FF);
+    return (int64_t)ud > 0 && (unsigned)(ed - 1) < 2046u && en < 2047 && en - ed < 1000;
+}
+
+// num / den is positive, finite and not zero: both positive normal, exponents close
+__device__ __forceinline__ bool quotient_positive(double num, double den)
+{
+    const uint64_t un = sfp::bits(num);
+    const int en = (int)((un >> 52) & 0x7FF), ed = (int)((sfp::bits(den) >> 52) & 0x7FF);
+    return (int64_t)un > 0 && (unsigned)(en - 1) < 2046u && quotient_finite(num, den) && ed - en < 1000;
+}
+
 template <class T>
 __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, const Flux<T>& Fp,
                                           const Lag<T>& L1, const Lag<T>& L2, const Adv<T>& d01,
@@ -307,6 +351,23 @@ __device__ __forceinline__ Adv<T> advect2(const Flux<T>& Fm, const Flux<T>& Fk, 
     T Dx = qneg_if(dx + (up ? qneg_if(Fm.dtus, true) : Fp.dtus), up);
     const T Dx_l = up ? L1.W : L2.W;
     const T two_Dx_l = qtwice(Dx_l);
+    if constexpr (sizeof(T) == 8) {
+        // every slope a signed zero: the three quotients are not needed (exactly the same result)
+        const Adv<T> dm = up ? d01 : d12, dp = up ? d12 : d23;
+        if (ARMON_SOFT_FP64 && slope_is_zero(dm.r, dp.r) && slope_is_zero(dm.ra, dp.ra) &&
+            slope_is_zero(dm.ro, dp.ro) && slope_is_zero(dm.rE, dp.rE) &&
+            quotient_positive(two_Dx_l, up ? s01 : s12) && quotient_positive(two_Dx_l, up ? s12 : s23) &&
+            quotient_finite(Dx, two_Dx_l)) {
+            const uint64_t sx = sfp::bits(Dx) >> 63;
+            const auto prod = [&](T d_p) { return sfp::from_bits(((sfp::bits(d_p) >> 63) ^ sx) << 63); };
+            Adv<T> a;
+            a.r = qmul<6>(disp, (up ? L1.rho : L2.rho) - prod(dp.r));
+            a.ra = qmul<6>(disp, (up ? L1.rua : L2.rua) - prod(dp.ra));
+            a.ro = qmul<6>(disp, (up ? L1.ruo : L2.ruo) - prod(dp.ro));
+            a.rE = qmul<6>(disp, (up ? L1.rE : L2.rE) - prod(dp.rE));
+            return a;
+        }
+    }
     T r_m = qdiv_at<6>(two_Dx_l, up ? s01 : s12);    // 2 Dx_l / (Dx_l + Dx_lm)
     T r_p = qdiv_at<6>(two_Dx_l, up ? s12 : s23);    // 2 Dx_l / (Dx_l + Dx_lp)
     T slope_r = slope_minmod(up ? d01.r : d12.r, up ? d12.r : d23.r, r_m, r_p);

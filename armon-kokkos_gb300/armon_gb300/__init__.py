@@ -49,7 +49,8 @@ class Params(C.Structure):
 
 class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("seg_len", C.c_int32),
-                ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("unit_order", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class BatchOpts(C.Structure):
@@ -131,6 +132,7 @@ def lib() -> C.CDLL:
     L.armon_solver_kernel_launches.argtypes = [S]
     L.armon_solver_kernel_launches.restype = C.c_int64
     L.armon_solver_tiling.argtypes = [S, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.armon_solver_block_lines.argtypes = [S]
     L.armon_solve_host.argtypes = [P, C.POINTER(SolverOpts), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), P]
     B = C.c_void_p
     L.armon_batch_opts_default.argtypes = [C.POINTER(BatchOpts)]
@@ -230,7 +232,8 @@ class Solver:
     """A domain resident in HBM with the fused time loop (armon_solver_* of include/armon_gb300.h)."""
 
     def __init__(self, params: Params | Case, precision: int = 64, stream: int | None = None,
-                 cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 0):
+                 cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 0,
+                 unit_order: int = 0):
         L = lib()
         self.params = make_params(params) if isinstance(params, Case) else params
         o = SolverOpts()
@@ -240,6 +243,7 @@ class Solver:
         o.seg_len = seg_len
         o.block_lines = block_lines
         o.materialize_eos = materialize_eos
+        o.unit_order = unit_order
         self.opts = o
         h = C.c_void_p()
         check(L.armon_solver_create(C.byref(self.params), C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
@@ -307,6 +311,10 @@ class Solver:
         sl, nb = (C.c_int32 * 2)(), (C.c_int32 * 2)()
         check(lib().armon_solver_tiling(self._h, sl, nb))
         return (sl[0], sl[1]), (nb[0], nb[1])
+
+    def block_lines(self) -> int:
+        """Lines (threads) per block of the fused pass."""
+        return int(lib().armon_solver_block_lines(self._h))
 
 
 def real_cells(p: Params, a: np.ndarray) -> np.ndarray:

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <string>
@@ -51,6 +52,10 @@ struct armon_solver {
     int tuned_seg[2] = {0, 0};      // measured segment lengths per axis (0: the model's)
     bool tuned = false;
     double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
+    bool ordered = true;            // longest-first dispatch of each pass's units
+    uint32_t* d_order = nullptr;    // per axis: order_cap unit indices, then order_cap costs
+    uint32_t* d_cost = nullptr;
+    int order_cap = 0;
 };
 
 namespace {
@@ -79,10 +84,110 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
                                  s->o.materialize_eos, a);
 }
 
+// Longest-first order of each axis's units from the SM cycles each took in its last pass: a
+// counting sort into kOrderClasses classes of cost / (max + 1), the most expensive class first.
+// One block per axis.  Which block takes which unit never changes a result (units are independent
+// and the dt partials are reduced by maximum), so the order within a class is left to the atomics.
+constexpr int kOrderClasses = 64;
+
+__global__ void order_units_kernel(const uint32_t* __restrict__ cost, uint32_t* __restrict__ order, int cap, int n0,
+                                   int n1)
+{
+    const int n = blockIdx.x == 0 ? n0 : n1;
+    cost += (size_t)blockIdx.x * cap;
+    order += (size_t)blockIdx.x * cap;
+    __shared__ unsigned start[kOrderClasses];
+    __shared__ unsigned wmax[32];
+    __shared__ unsigned top;
+    unsigned m = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, cost[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    for (int c = threadIdx.x; c < kOrderClasses; c += blockDim.x) start[c] = 0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned v = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0u;
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) top = v;
+    }
+    __syncthreads();
+    const uint64_t scale = (uint64_t)top + 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        atomicAdd(&start[kOrderClasses - 1 - (int)((uint64_t)cost[i] * kOrderClasses / scale)], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned sum = 0;
+        for (int c = 0; c < kOrderClasses; c++) { const unsigned h = start[c]; start[c] = sum; sum += h; }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = kOrderClasses - 1 - (int)((uint64_t)cost[i] * kOrderClasses / scale);
+        order[atomicAdd(&start[c], 1u)] = (uint32_t)i;
+    }
+}
+
+// order[axis][i] = i, cost = 0
+__global__ void reset_order_kernel(uint32_t* __restrict__ order, uint32_t* __restrict__ cost, int cap)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * cap; i += gridDim.x * blockDim.x) {
+        order[i] = (uint32_t)(i % cap);
+        cost[i] = 0;
+    }
+}
+
 int sync_state(armon_solver* s)
 {
     CUDA_TRY(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return ARMON_OK;
+}
+
+int axis_blocks(const armon_solver* s, int axis)
+{
+    return s->fp32 ? s->a32.geom[axis].blocks : s->a64.geom[axis].blocks;
+}
+
+// The next passes' unit order from the costs the last passes recorded.
+int launch_order(armon_solver* s)
+{
+    if (!s->ordered) return ARMON_OK;
+    order_units_kernel<<<2, 1024, 0, s->stream>>>(s->d_cost, s->d_order, s->order_cap, axis_blocks(s, 0),
+                                                  axis_blocks(s, 1));
+    CUDA_TRY(cudaGetLastError());
+    s->launches++;
+    return ARMON_OK;
+}
+
+// (Re)sizes the order and cost arrays for the current tiling, points the sweep arguments at them
+// and starts from index order.
+int prepare_order(armon_solver* s)
+{
+    if (!s->ordered) return ARMON_OK;
+    const int need = std::max(axis_blocks(s, 0), axis_blocks(s, 1));
+    if (need > s->order_cap) {
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        cudaFree(s->d_order);
+        cudaFree(s->d_cost);
+        s->d_order = s->d_cost = nullptr;
+        s->order_cap = 0;
+        cudaError_t e = cudaMalloc(&s->d_order, sizeof(uint32_t) * 2 * (size_t)need);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_cost, sizeof(uint32_t) * 2 * (size_t)need);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return ARMON_ERR_NOMEM;
+        }
+        s->order_cap = need;
+    }
+    for (int axis = 0; axis < 2; axis++) {
+        uint32_t* o = s->d_order + (size_t)axis * s->order_cap;
+        uint32_t* c = s->d_cost + (size_t)axis * s->order_cap;
+        if (s->fp32) { s->a32.geom[axis].order = o; s->a32.geom[axis].cost = c; }
+        else { s->a64.geom[axis].order = o; s->a64.geom[axis].cost = c; }
+    }
+    reset_order_kernel<<<std::max(1, std::min(s->sm_count * 4, (2 * s->order_cap + 255) / 256)), 256, 0, s->stream>>>(
+        s->d_order, s->d_cost, s->order_cap);
+    CUDA_TRY(cudaGetLastError());
+    s->launches++;
     return ARMON_OK;
 }
 
@@ -102,6 +207,8 @@ int enqueue_direct(armon_solver* s, int n_cycles)
             if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
             s->launches++;
         }
+        int rc = launch_order(s);
+        if (rc != ARMON_OK) return rc;
     }
     return ARMON_OK;
 }
@@ -130,7 +237,7 @@ int enqueue(armon_solver* s, int n_cycles)
         if (rc != ARMON_OK) return rc;
         while (n_cycles >= s->graph_cycles) {
             CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
-            s->launches += (int64_t)s->graph_cycles * s->npass;
+            s->launches += (int64_t)s->graph_cycles * (s->npass + (s->ordered ? 1 : 0));
             n_cycles -= s->graph_cycles;
         }
     }
@@ -165,13 +272,21 @@ int ensure_stage(armon_solver* s)
 
 // Tiling of a lone domain, measured.  With the GPU to itself, the best segment length depends on
 // more than the cells a thread walks (how full the last wave of blocks is, how many blocks share an
-// SM, cache traffic), so before the first cycle the solver times the pass of cycle 0 -- which reads
-// one buffer set, writes the other and leaves the step state alone -- with a few candidate tilings
-// (the model's, and segments aiming at 1, 2, 3, 4, 6 and 8 waves of resident blocks), keeps the
-// fastest for both axes and caches it per geometry for the process.  Results never depend on the
-// tiling.  Domains under 2^20 cells, single-pass splittings and a caller-fixed seg_len are left to
-// the model.
-std::map<std::array<int, 7>, std::array<int, 2>> g_tilings;
+// SM, how unevenly the units cost once wave fronts have formed, cache traffic), so begin_loop times
+// a few candidate tilings -- the model's, and segments aiming at 1, 2, 3, 4, 6 and 8 waves of
+// resident blocks, for blocks of 128 and of 32 lines unless the caller fixed the block -- keeps the
+// fastest and caches it per geometry for the process.  The candidates run real cycles from 32
+// cycles into the run, on a copy of the state that is put back afterwards, so the time loop then
+// starts from the very same state (when the device has no room for the copy they are timed on the
+// pass of cycle 0, which reads one buffer set, writes the other and leaves the step state alone).
+// Results never depend on the tiling.  Domains under 2^20 cells, single-pass splittings and a
+// caller-fixed seg_len are left to the model.
+struct Tiling {
+    int seg[2];
+    int block;
+    bool operator==(const Tiling& o) const { return seg[0] == o.seg[0] && seg[1] == o.seg[1] && block == o.block; }
+};
+std::map<std::array<int, 7>, Tiling> g_tilings;
 std::mutex g_tilings_mu;
 
 int launch_pass0(armon_solver* s)
@@ -189,13 +304,14 @@ int launch_pass0(armon_solver* s)
     return ARMON_OK;
 }
 
-void refill(armon_solver* s)
+int refill(armon_solver* s)
 {
     if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
         s->graph = nullptr;
     }
+    return prepare_order(s);
 }
 
 int ensure_partials(armon_solver* s)
@@ -210,76 +326,153 @@ int ensure_partials(armon_solver* s)
     return ARMON_OK;
 }
 
+void set_tiling(armon_solver* s, const Tiling& t)
+{
+    s->tuned_seg[0] = t.seg[0];
+    s->tuned_seg[1] = t.seg[1];
+    s->block = t.block;
+}
+
+// Times each candidate tiling: on developed cycles (`cycles` > 0: one warm-up cycle that records
+// the unit costs, then `cycles` timed cycles) or on the pass of the current cycle (`cycles` == 0:
+// warm-up pass, then two timed passes).  Returns the index of the fastest in *best.
+int time_candidates(armon_solver* s, const std::vector<Tiling>& cand, int cycles, size_t* best)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    *best = 0;
+    int rc = ARMON_OK;
+    for (size_t i = 0; i < cand.size() && rc == ARMON_OK; i++) {
+        set_tiling(s, cand[i]);
+        rc = refill(s);
+        if (rc == ARMON_OK) rc = ensure_partials(s);
+        if (rc == ARMON_OK) rc = cycles > 0 ? enqueue_direct(s, 1) : launch_pass0(s);
+        if (rc == ARMON_OK && cycles == 0) rc = launch_order(s);
+        if (rc == ARMON_OK && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK) {
+            if (cycles > 0) rc = enqueue_direct(s, cycles);
+            else for (int k = 0; k < 2 && rc == ARMON_OK; k++) rc = launch_pass0(s);
+        }
+        if (rc == ARMON_OK && cudaEventRecord(e1, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        float ms = 0;
+        if (rc == ARMON_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK && ms < best_ms) { best_ms = ms; *best = i; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+// The arrays a cycle changes (rho, umat, vmat, Emat, pmat, cmat, gmat), saved so that the tiling
+// can be measured on real cycles and the time loop then restarts from the saved state bit for bit.
+constexpr int kSnapArrays[7] = {2, 3, 4, 5, 6, 7, 8};
+constexpr int kTuneWarmCycles = 32;   // cycles run before the measurement, to develop the flow
+constexpr int kTuneCycles = 2;        // timed cycles per candidate
+
 int tune_tiling(armon_solver* s)
 {
     if (s->tuned || s->o.seg_len > 0 || s->npass < 2) return ARMON_OK;
     s->tuned = true;
     const armon_params& p = s->p;
     if ((int64_t)p.nx * p.ny < (1 << 20)) return ARMON_OK;
-    const std::array<int, 7> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting, s->block};
+    const std::array<int, 7> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting,
+                                 s->o.block_lines};
     {
         std::lock_guard<std::mutex> lk(g_tilings_mu);
         auto it = g_tilings.find(key);
         if (it != g_tilings.end()) {
-            s->tuned_seg[0] = it->second[0];
-            s->tuned_seg[1] = it->second[1];
-            refill(s);
-            return ensure_partials(s);
+            set_tiling(s, it->second);
+            int rc = refill(s);
+            return rc != ARMON_OK ? rc : ensure_partials(s);
         }
     }
-    const StepState& st = *s->h_state;
+    const StepState st = *s->h_state;
     if (!(st.status == STATUS_RUNNING && st.time < p.max_time && st.cycle < p.max_cycles)) return ARMON_OK;
 
-    // candidates: the model's tiling, then segments aiming at w waves of resident blocks per axis
-    const int slots = s->sm_count * sweep_blocks_per_sm(s->fp32, p.scheme, p.projection, s->block);
+    // candidates per block size: the model's tiling, then segments aiming at w waves of resident
+    // blocks per axis
     const int halo = stencil_reach(&p);
-    std::vector<std::array<int, 2>> cand;
-    std::array<int, 2> model;
-    for (int axis = 0; axis < 2; axis++) {
-        const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
-        model[axis] = choose_segments(n, nl, s->block, halo, s->sm_count, 0).seg_len;
-    }
-    cand.push_back(model);
-    for (int w : {1, 2, 3, 4, 6, 8}) {
-        std::array<int, 2> c;
+    std::vector<Tiling> cand;
+    std::vector<int> blocks;
+    if (s->o.block_lines > 0) blocks.push_back(s->block); else blocks = {128, 32};
+    for (int block : blocks) {
+        const int slots = s->sm_count * sweep_blocks_per_sm(s->fp32, p.scheme, p.projection, block);
+        Tiling model{{0, 0}, block};
         for (int axis = 0; axis < 2; axis++) {
             const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
-            const AxisTiling t = axis_tiling(n, nl, s->block, n);   // one segment: nlb, spb
-            const int per_line = std::max(1, (int)std::lround(double(w) * slots * t.spb / t.nlb));
-            c[axis] = std::max(16, (n + per_line - 1) / per_line);
+            model.seg[axis] = choose_segments(n, nl, block, halo, s->sm_count, 0).seg_len;
         }
-        if (std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+        cand.push_back(model);
+        for (int w : {1, 2, 3, 4, 6, 8}) {
+            Tiling c{{0, 0}, block};
+            for (int axis = 0; axis < 2; axis++) {
+                const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
+                const AxisTiling t = axis_tiling(n, nl, block, n);   // one segment: nlb, spb
+                const int per_line = std::max(1, (int)std::lround(double(w) * slots * t.spb / t.nlb));
+                c.seg[axis] = std::max(16, (n + per_line - 1) / per_line);
+            }
+            if (std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+        }
     }
 
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    CUDA_TRY(cudaEventCreate(&e0));
-    CUDA_TRY(cudaEventCreate(&e1));
-    float best_ms = 1e30f;
-    std::array<int, 2> best = model;
+    // On developed cycles when the device has room for a copy of the state, else on the pass of
+    // cycle 0.  The measured cycles run past the caller's max_cycles / max_time if need be: the
+    // copy is put back afterwards and the loop bounds with it.
+    const int need = kTuneWarmCycles + (int)cand.size() * (1 + kTuneCycles);
+    void* snap[7] = {};
+    bool developed = true;
+    const size_t bytes = (size_t)p.nb_cells * s->elem;
+    for (int k = 0; k < 7 && developed; k++)
+        if (cudaMalloc(&snap[k], bytes) != cudaSuccess) { cudaGetLastError(); developed = false; }
+    size_t best = 0;
     int rc = ARMON_OK;
-    for (const auto& c : cand) {
-        s->tuned_seg[0] = c[0];
-        s->tuned_seg[1] = c[1];
-        refill(s);
-        rc = launch_pass0(s);                                    // warm-up
-        if (rc == ARMON_OK && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        for (int k = 0; k < 2 && rc == ARMON_OK; k++) rc = launch_pass0(s);
-        if (rc == ARMON_OK && cudaEventRecord(e1, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        float ms = 0;
-        if (rc == ARMON_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc != ARMON_OK) break;
-        if (ms < best_ms) { best_ms = ms; best = c; }
+    if (developed) {
+        const int32_t max_cycles = s->p.max_cycles;
+        const double max_time = s->p.max_time;
+        s->p.max_cycles = std::numeric_limits<int32_t>::max();
+        s->p.max_time = std::numeric_limits<double>::infinity();
+        rc = refill(s);
+        for (int k = 0; k < 7 && rc == ARMON_OK; k++)
+            if (cudaMemcpyAsync(snap[k], s->arr[kSnapArrays[k]], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
+                rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK) rc = enqueue_direct(s, kTuneWarmCycles);
+        if (rc == ARMON_OK) rc = time_candidates(s, cand, kTuneCycles, &best);
+        // valid only if every cycle ran (the loop may have reached max_time)
+        if (rc == ARMON_OK) rc = sync_state(s);
+        const StepState& now = *s->h_state;
+        const bool ran = rc == ARMON_OK && now.status == STATUS_RUNNING && now.cycle == st.cycle + need;
+        s->p.max_cycles = max_cycles;
+        s->p.max_time = max_time;
+        // restore: set 0 and p, c, g from the copy, set 1 = set 0, the step state as it was
+        for (int k = 0; k < 7 && rc == ARMON_OK; k++)
+            if (cudaMemcpyAsync(s->arr[kSnapArrays[k]], snap[k], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
+                rc = ARMON_ERR_CUDA;
+        for (int k = 0; k < 4 && rc == ARMON_OK; k++)
+            if (cudaMemcpyAsync(s->arr[11 + k], s->arr[2 + k], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
+                rc = ARMON_ERR_CUDA;
+        *s->h_state = st;
+        if (rc == ARMON_OK &&
+            cudaMemcpyAsync(s->d_state, s->h_state, sizeof(StepState), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+            rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
+        if (rc == ARMON_OK && !ran) developed = false;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc != ARMON_OK) { set_error("tiling measurement failed"); return rc; }
-    s->tuned_seg[0] = best[0];
-    s->tuned_seg[1] = best[1];
-    refill(s);
+    for (void* a : snap) if (a) cudaFree(a);
+    if (rc == ARMON_OK && !developed) rc = time_candidates(s, cand, 0, &best);
+    if (rc != ARMON_OK) {
+        set_error("tiling measurement failed");
+        refill(s);
+        return rc;
+    }
+    set_tiling(s, cand[best]);
+    rc = refill(s);
+    if (rc != ARMON_OK) return rc;
     {
         std::lock_guard<std::mutex> lk(g_tilings_mu);
-        g_tilings[key] = best;
+        g_tilings[key] = cand[best];
     }
     return ensure_partials(s);
 }
@@ -326,6 +519,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     s->fp32 = s->o.precision == 32;
     s->elem = s->fp32 ? 4 : 8;
     s->block = s->o.block_lines > 0 ? s->o.block_lines : 128;
+    s->ordered = s->o.unit_order >= 0;
     if (s->block % 32 != 0 || s->block > 128) { delete s; set_error("block_lines must be a multiple of 32, at most 128"); return ARMON_ERR_PARAMS; }
     s->graph_cycles = s->o.cycles_per_graph;
     s->npass = passes_per_cycle(p->axis_splitting);
@@ -372,6 +566,8 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
     std::memset(s->h_state, 0, sizeof(StepState));
     if (s->fp32) fill_geom(s, s->a32); else fill_geom(s, s->a64);
+    rc = prepare_order(s);
+    if (rc != ARMON_OK) { armon_solver_destroy(s); return rc; }
     *out = s;
     return ARMON_OK;
 }
@@ -399,6 +595,8 @@ void armon_solver_destroy(armon_solver* s)
     if (s->d_partials) cudaFree(s->d_partials);
     if (s->d_cons) cudaFree(s->d_cons);
     if (s->stage) cudaFree(s->stage);
+    if (s->d_order) cudaFree(s->d_order);
+    if (s->d_cost) cudaFree(s->d_cost);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
@@ -604,6 +802,8 @@ int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2])
     }
     return ARMON_OK;
 }
+
+int armon_solver_block_lines(const armon_solver* s) { return s->block; }
 
 int armon_solve_host(const armon_params* p, const armon_solver_opts* opts, const double* const in[4],
                      double* const out[5], armon_params* final_state)

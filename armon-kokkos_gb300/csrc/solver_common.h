@@ -54,9 +54,9 @@ inline AxisTiling axis_tiling(int n, int nlines, int block, int seg_len)
     return t;
 }
 
-// Segments along the axis of one domain that has the GPU to itself: minimise (most blocks on one
-// SM) x (cells a thread walks, halo included) over the segment count, with segments of at least
-// 16 cells.  forced > 0 imposes the segment length.
+// Segments along the axis of one domain that has the GPU to itself: minimise (most threads on one
+// SM, in units of 128) x (cells a thread walks, halo included) over the segment count, with
+// segments of at least 16 cells.  forced > 0 imposes the segment length.
 inline AxisTiling choose_segments(int n, int nlines, int block, int halo, int sms, int forced)
 {
     if (forced > 0) return axis_tiling(n, nlines, block, forced);
@@ -66,7 +66,7 @@ inline AxisTiling choose_segments(int n, int nlines, int block, int halo, int sm
         int sl = (n + ns - 1) / ns;
         if ((int64_t)sl * (ns - 1) >= n) continue;
         AxisTiling t = axis_tiling(n, nlines, block, sl);
-        double per_sm = std::ceil(double(t.blocks) / sms);
+        double per_sm = std::ceil(double(t.blocks) * block / (128.0 * sms));
         double cost = per_sm * (sl + 1.2 * halo);
         if (cost < best - 1e-9) { best = cost; best_seg = sl; }
     }
@@ -156,6 +156,8 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, const 
         g.dx_pow2 = is_pow2(double(g.dx)) ? 1 : 0;
         g.inv_dx = g.dx_pow2 ? T(1.0 / double(g.dx)) : T(0);
         g.dx_log2 = g.dx_pow2 ? std::ilogb(double(g.dx)) : 0;
+        g.order = nullptr;
+        g.cost = nullptr;
     }
     a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
     a.sw = p.stencil_width;

@@ -96,6 +96,10 @@ struct AxisGeom {
     int32_t dx_log2;    // dx == 2^dx_log2 when dx_pow2
     int32_t lpb;        // lines per block: a multiple of 32 dividing blockDim.x
     int32_t spb;        // segments per block: blockDim.x / lpb (narrow domains fill a block with segments)
+    // Longest-first dispatch (optional, both NULL when unused): block b of the launch works on unit
+    // order[b] of the axis, and records the SM cycles that unit took in cost[unit].
+    const uint32_t* order;
+    uint32_t* cost;
 };
 
 template <class T>
@@ -485,14 +489,19 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
     acc.init();
     const T gamma_m1 = A.gamma - 1;
 
-    // block blk = (line block lb, segment block sb); warp-aligned groups of lpb threads take spb
-    // consecutive segments of the same lpb lines
-    const int lb = blk % max(g.nlb, 1);
-    const int sb = blk / max(g.nlb, 1);
+    // unit u = (line block lb, segment block sb); warp-aligned groups of lpb threads take spb
+    // consecutive segments of the same lpb lines.  Units are independent, so which block takes which
+    // unit changes nothing in the results; with an order, the units that took longest in the
+    // previous cycle start first and the cheap ones fill the tail of the launch.
+    const bool has_unit = blk < g.blocks;
+    const int u = (g.order != nullptr && has_unit) ? (int)__ldg(&g.order[blk]) : blk;
+    const long long clock_start = clock64();
+    const int lb = u % max(g.nlb, 1);
+    const int sb = u / max(g.nlb, 1);
     const int sub = (int)threadIdx.x / g.lpb;
     const int seg = sb * g.spb + sub;
     const int line = lb * g.lpb + (int)threadIdx.x % g.lpb;
-    const bool active = blk < g.blocks && line < g.nlines && seg < g.nseg && sub < g.spb;
+    const bool active = has_unit && line < g.nlines && seg < g.nseg && sub < g.spb;
 
     if (active) {
         const int n = g.n, sw = A.sw;
@@ -619,6 +628,11 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         }
     }
 
+    if (g.cost != nullptr) {
+        __syncthreads();
+        if (threadIdx.x == 0 && has_unit)
+            g.cost[u] = (uint32_t)min(clock64() - clock_start, (long long)0xFFFFFFFFu);
+    }
     if constexpr (LAST) {
         acc.finish();
         commit_cycle(A, acc, st, cd, blk, nblk);

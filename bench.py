@@ -285,7 +285,8 @@ def run_gpu(args) -> None:
     # a dedicated stream: the solver launches on it and the CUDA events are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len)
+    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len,
+                 block_lines=args.block_lines)
     s.init_test()
     s.enqueue_cycles(W)
     torch.cuda.synchronize()
@@ -298,6 +299,7 @@ def run_gpu(args) -> None:
     barrier()
     launches0 = s.kernel_launches
     tiling = s.tiling()
+    block_lines = s.block_lines()
     sampler = ClockSampler() if rank == 0 else None
     if sampler:
         sampler.start()
@@ -325,7 +327,7 @@ def run_gpu(args) -> None:
     case_e2e.nx, case_e2e.ny = nx, ny
     case_e2e.max_cycles = K
     se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
-                  seg_len=args.seg_len)
+                  seg_len=args.seg_len, block_lines=args.block_lines)
     se.init_test()
     outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
             for k in ("rho", "umat", "vmat", "Emat", "pmat")}
@@ -355,7 +357,8 @@ def run_gpu(args) -> None:
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64" if prec == 64 else "f32", "data": "synthetic",
-               "config": dict(config(nx, ny, world, prec), seg_len=list(tiling[0]), blocks=list(tiling[1])),
+               "config": dict(config(nx, ny, world, prec), seg_len=list(tiling[0]), blocks=list(tiling[1]),
+                             block_lines=block_lines),
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_source": peak_kind,
                             "traffic": (tr * cells if tr else None),
@@ -383,12 +386,12 @@ def run_gpu(args) -> None:
         torch.distributed.destroy_process_group()
 
 
-def plain_solve(A, spec, precision: int, graph: int) -> tuple[float, int]:
+def plain_solve(A, spec, precision: int, graph: int, block_lines: int = 0) -> tuple[float, int]:
     """One domain on the plain single-domain path (its own solver: init, upload of the initial
     fields, time loop); returns the seconds of its time loop and its cell-updates."""
     import torch
 
-    with A.Solver(spec.params(), precision=precision, cycles_per_graph=graph) as s:
+    with A.Solver(spec.params(), precision=precision, cycles_per_graph=graph, block_lines=block_lines) as s:
         s.init_test()
         for k, a in spec.initial_state().items():
             s.upload(k, a)
@@ -415,13 +418,13 @@ def run_batch(args) -> None:
     torch.cuda.set_device(0)
     # plain path (domains one at a time; the first is a warm-up)
     plain_secs, plain_work = 0.0, 0
-    plain_solve(A, specs[0], 64, args.graph)
+    plain_solve(A, specs[0], 64, args.graph, args.block_lines)
     for sp in specs:
-        s_, w_ = plain_solve(A, sp, 64, args.graph)
+        s_, w_ = plain_solve(A, sp, 64, args.graph, args.block_lines)
         plain_secs += s_
         plain_work += w_
     # batched
-    with A.Batch(precision=64, cycles_per_graph=8) as b:
+    with A.Batch(precision=64, cycles_per_graph=8, block_lines=args.block_lines or 128) as b:
         ids = [b.add_sod(sp.params(), sp.sod_interface()) for sp in specs]
         b.poll()
         launches0 = b.kernel_launches
@@ -535,6 +538,7 @@ def main():
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
     ap.add_argument("--seg-len", type=int, default=0, help="cells per thread along the sweep axis (0 = automatic)")
+    ap.add_argument("--block-lines", type=int, default=0, help="threads (lines) per block of the axis pass (0 = automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--accuracy-cycles", type=int, default=100,

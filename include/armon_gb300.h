@@ -88,7 +88,10 @@ typedef struct armon_solver_opts {
     int32_t materialize_eos;  /* write p, c, g of the real cells on every pass (1) or only on the
                                  last pass of a cycle (0, default): the arrays the time loop leaves
                                  are the same, since every pass's EOS overwrites the previous one */
-    int32_t reserved[3];
+    int32_t unit_order;       /* 0 (default): each pass launches its blocks longest first, by the time
+                                 each took in the previous cycle (results do not depend on it);
+                                 -1: in index order */
+    int32_t reserved[2];
 } armon_solver_opts;
 
 void armon_solver_opts_default(armon_solver_opts* o);
@@ -146,6 +149,8 @@ int64_t armon_solver_kernel_launches(armon_solver* s);
  * candidate tilings, timed on its cycle-0 pass at the start of its first time loop (no change to
  * the state or the results); smaller domains use the cost model. */
 int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2]);
+/* Lines (threads) per block of the fused pass: the caller's block_lines, or the measured choice. */
+int armon_solver_block_lines(const armon_solver* s);
 
 /* ---- batches: many independent domains advanced together (no counterpart in the reference;
  *      each domain follows time_loop, src/armon_2D.cpp:327-386, on its own) ---- */

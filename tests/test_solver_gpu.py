@@ -192,3 +192,45 @@ def test_measured_tiling_keeps_results():
         for k in FIELDS:
             assert np.array_equal(out[0][k].view(np.int64), other[k].view(np.int64)), k
 
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_longest_first_dispatch_keeps_results(precision):
+    # blocks launched in the order of the previous cycle's unit costs give the same bits as blocks
+    # in index order, for 128- and 32-thread blocks and an alternating splitting
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=384, ny=320, cfl=0.6,
+                  max_cycles=40, max_time=1e9, test_option=0.04, splitting="SequentialSym")
+    ref = None
+    for block, order in ((128, -1), (128, 0), (32, 0), (64, 0)):
+        s, p, status = run_solver(case, precision=precision, block_lines=block, seg_len=24, unit_order=order,
+                                  cycles_per_graph=8)
+        with s:
+            assert status == 0 and p.cycle == 40
+            fields = {k: s.download(k) for k in FIELDS}
+        if ref is None:
+            ref = fields
+            continue
+        for k in FIELDS:
+            assert np.array_equal(ref[k].view(np.int64), fields[k].view(np.int64)), (block, order, k)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_tiling_measured_on_developed_cycles_restores_the_state(precision):
+    # with room in the loop, the solver measures its candidate tilings on real cycles from a copy of
+    # the state and restarts from that copy: the run that follows equals one with a fixed tiling
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=1024, ny=1040, cfl=0.6,
+                  max_cycles=200, max_time=1e9, test_option=0.04)
+    out = []
+    for seg in (0, 128):
+        with A.Solver(case, precision=precision, seg_len=seg) as s:
+            s.init_test()
+            p, status = s.state()
+            assert status == 0 and p.cycle == 0 and p.time == 0.0
+            s.run(cycle_limit=12)
+            p, status = s.state()
+            assert status == 0 and p.cycle == 12
+            out.append(({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt))
+    (a, ta, da), (b, tb, db) = out
+    assert ta == tb and da == db
+    for k in FIELDS:
+        assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k

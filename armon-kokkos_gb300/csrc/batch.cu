@@ -17,6 +17,7 @@
 #include "armon_gb300.h"
 #include "host_common.h"
 #include "launch.h"
+#include "order.cuh"
 #include "solver_common.h"
 
 using namespace armon;
@@ -89,6 +90,10 @@ struct armon_batch {
     cudaGraphExec_t graph = nullptr;
     int64_t bytes = 0;
     int64_t launches = 0;
+    bool ordered = true;          // longest-first dispatch of each pass's blocks
+    uint32_t* d_order = nullptr;  // npass arrays of order_cap block indices
+    uint32_t* d_cost = nullptr;   // npass arrays of order_cap costs
+    int order_cap = 0;
 };
 
 namespace {
@@ -202,6 +207,25 @@ int rebuild_t(armon_batch* b)
         offsets[k + 1] = offsets[k] + nb;
     }
     b->total_blocks = offsets.back();
+    if (b->ordered && !b->table.empty()) {
+        // a new table: index order until its blocks have costs
+        if (b->total_blocks > b->order_cap) {
+            CUDA_TRY(cudaStreamSynchronize(b->stream));
+            cudaFree(b->d_order);
+            cudaFree(b->d_cost);
+            b->d_order = b->d_cost = nullptr;
+            b->order_cap = 0;
+            const int cap = b->total_blocks + b->total_blocks / 4;
+            CUDA_TRY(cudaMalloc(&b->d_order, sizeof(uint32_t) * kMaxOrderArrays * (size_t)cap));
+            CUDA_TRY(cudaMalloc(&b->d_cost, sizeof(uint32_t) * kMaxOrderArrays * (size_t)cap));
+            b->order_cap = cap;
+        }
+        const int total = b->order_cap * b->npass;
+        reset_order_kernel<<<std::max(1, std::min(b->sm_count * 4, (total + 255) / 256)), 256, 0, b->stream>>>(
+            b->d_order, b->d_cost, b->order_cap, b->npass);
+        CUDA_TRY(cudaGetLastError());
+        b->launches++;
+    }
     if (!b->table.empty()) {
         CUDA_TRY(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(SweepArgs<T>), cudaMemcpyHostToDevice,
                                  b->stream));
@@ -275,12 +299,23 @@ int enqueue_direct(armon_batch* b, int n)
     for (int c = 0; c < n; c++) {
         for (int k = 0; k < b->npass; k++) {
             bool last = k == b->npass - 1;
+            BatchOrder ord{nullptr, nullptr};
+            if (b->ordered) {
+                ord.order = b->d_order + (size_t)k * b->order_cap;
+                ord.cost = b->d_cost + (size_t)k * b->order_cap;
+            }
             cudaError_t e = b->fp32
-                ? launch_sweep_batch((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                ? launch_sweep_batch((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks, k, ord,
                                      b->scheme, b->proj, last, b->o.block_lines, b->stream)
-                : launch_sweep_batch((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                : launch_sweep_batch((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks, k, ord,
                                      b->scheme, b->proj, last, b->o.block_lines, b->stream);
             if (e != cudaSuccess) return cuda_fail(e, "batch sweep launch");
+            b->launches++;
+        }
+        if (b->ordered) {
+            UnitCounts counts{{b->total_blocks, b->total_blocks, b->total_blocks, b->total_blocks}};
+            order_units_kernel<<<b->npass, 1024, 0, b->stream>>>(b->d_cost, b->d_order, b->order_cap, counts);
+            CUDA_TRY(cudaGetLastError());
             b->launches++;
         }
     }
@@ -324,7 +359,7 @@ int enqueue(armon_batch* b, int n)
                 b->tune.launched = true;
                 b->tune.work = double(table_cells(b)) * gc;
             }
-            b->launches += (int64_t)gc * b->npass;
+            b->launches += (int64_t)gc * (b->npass + (b->ordered ? 1 : 0));
             n -= gc;
         }
     }
@@ -383,6 +418,7 @@ int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch**
     }
     b->fp32 = b->o.precision == 32;
     b->elem = b->fp32 ? 4 : 8;
+    b->ordered = b->o.unit_order >= 0;
     if (b->o.waves > 0) b->waves = b->o.waves;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -434,6 +470,8 @@ void armon_batch_destroy(armon_batch* b)
     if (b->h_states) cudaFreeHost(b->h_states);
     if (b->d_args) cudaFree(b->d_args);
     if (b->d_offsets) cudaFree(b->d_offsets);
+    if (b->d_order) cudaFree(b->d_order);
+    if (b->d_cost) cudaFree(b->d_cost);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);

@@ -18,9 +18,9 @@ cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool l
 
 // Fused axis pass over many domains (sweep_batch_kernel): doms / offsets are device arrays.
 cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
-                               int scheme, int proj, bool last, int block, cudaStream_t st);
+                               BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st);
 cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks, int pass,
-                               int scheme, int proj, bool last, int block, cudaStream_t st);
+                               BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st);
 
 // Blocks of the batch kernel (last pass of a cycle) resident on one SM.
 int sweep_blocks_per_sm_f64(int scheme, int proj, int block);

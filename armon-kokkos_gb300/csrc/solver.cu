@@ -20,6 +20,7 @@
 #include "armon_gb300.h"
 #include "host_common.h"
 #include "launch.h"
+#include "order.cuh"
 #include "solver_common.h"
 
 using namespace armon;
@@ -84,57 +85,6 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
                                  s->o.materialize_eos, a);
 }
 
-// Longest-first order of each axis's units from the SM cycles each took in its last pass: a
-// counting sort into kOrderClasses classes of cost / (max + 1), the most expensive class first.
-// One block per axis.  Which block takes which unit never changes a result (units are independent
-// and the dt partials are reduced by maximum), so the order within a class is left to the atomics.
-constexpr int kOrderClasses = 64;
-
-__global__ void order_units_kernel(const uint32_t* __restrict__ cost, uint32_t* __restrict__ order, int cap, int n0,
-                                   int n1)
-{
-    const int n = blockIdx.x == 0 ? n0 : n1;
-    cost += (size_t)blockIdx.x * cap;
-    order += (size_t)blockIdx.x * cap;
-    __shared__ unsigned start[kOrderClasses];
-    __shared__ unsigned wmax[32];
-    __shared__ unsigned top;
-    unsigned m = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, cost[i]);
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
-    for (int c = threadIdx.x; c < kOrderClasses; c += blockDim.x) start[c] = 0;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        unsigned v = threadIdx.x < (blockDim.x >> 5) ? wmax[threadIdx.x] : 0u;
-        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (threadIdx.x == 0) top = v;
-    }
-    __syncthreads();
-    const uint64_t scale = (uint64_t)top + 1;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        atomicAdd(&start[kOrderClasses - 1 - (int)((uint64_t)cost[i] * kOrderClasses / scale)], 1u);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned sum = 0;
-        for (int c = 0; c < kOrderClasses; c++) { const unsigned h = start[c]; start[c] = sum; sum += h; }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int c = kOrderClasses - 1 - (int)((uint64_t)cost[i] * kOrderClasses / scale);
-        order[atomicAdd(&start[c], 1u)] = (uint32_t)i;
-    }
-}
-
-// order[axis][i] = i, cost = 0
-__global__ void reset_order_kernel(uint32_t* __restrict__ order, uint32_t* __restrict__ cost, int cap)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * cap; i += gridDim.x * blockDim.x) {
-        order[i] = (uint32_t)(i % cap);
-        cost[i] = 0;
-    }
-}
-
 int sync_state(armon_solver* s)
 {
     CUDA_TRY(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
@@ -151,8 +101,8 @@ int axis_blocks(const armon_solver* s, int axis)
 int launch_order(armon_solver* s)
 {
     if (!s->ordered) return ARMON_OK;
-    order_units_kernel<<<2, 1024, 0, s->stream>>>(s->d_cost, s->d_order, s->order_cap, axis_blocks(s, 0),
-                                                  axis_blocks(s, 1));
+    UnitCounts n{{axis_blocks(s, 0), axis_blocks(s, 1), 0, 0}};
+    order_units_kernel<<<2, 1024, 0, s->stream>>>(s->d_cost, s->d_order, s->order_cap, n);
     CUDA_TRY(cudaGetLastError());
     s->launches++;
     return ARMON_OK;
@@ -185,7 +135,7 @@ int prepare_order(armon_solver* s)
         else { s->a64.geom[axis].order = o; s->a64.geom[axis].cost = c; }
     }
     reset_order_kernel<<<std::max(1, std::min(s->sm_count * 4, (2 * s->order_cap + 255) / 256)), 256, 0, s->stream>>>(
-        s->d_order, s->d_cost, s->order_cap);
+        s->d_order, s->d_cost, s->order_cap, 2);
     CUDA_TRY(cudaGetLastError());
     s->launches++;
     return ARMON_OK;

@@ -164,19 +164,19 @@ static cudaError_t launch_sweep_t(const SweepArgs<T>& a, int scheme, int proj, b
 
 template <class T, int S, int P, bool L>
 static cudaError_t launch_batch_one(const SweepArgs<T>* doms, const int* offsets, int ndom, int grid, int pass,
-                                    int block, cudaStream_t st)
+                                    BatchOrder ord, int block, cudaStream_t st)
 {
-    sweep_batch_kernel<T, S, P, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass);
+    sweep_batch_kernel<T, S, P, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass, ord);
     return cudaGetLastError();
 }
 
 template <class T>
 static cudaError_t launch_sweep_batch_t(const SweepArgs<T>* doms, const int* offsets, int ndom, int grid, int pass,
-                                        int scheme, int proj, bool last, int block, cudaStream_t st)
+                                        BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st)
 {
 #define ARMON_B(S, P)                                                                                  \
-    return last ? launch_batch_one<T, S, P, true>(doms, offsets, ndom, grid, pass, block, st)          \
-                : launch_batch_one<T, S, P, false>(doms, offsets, ndom, grid, pass, block, st)
+    return last ? launch_batch_one<T, S, P, true>(doms, offsets, ndom, grid, pass, ord, block, st)     \
+                : launch_batch_one<T, S, P, false>(doms, offsets, ndom, grid, pass, ord, block, st)
     if (scheme == 1) {
         if (proj == 2) ARMON_B(1, 2);
         ARMON_B(1, 1);

@@ -649,11 +649,20 @@ __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_kernel(const
 // Many independent domains in one launch.  Domain d owns blocks [offsets[d], offsets[d+1]) of the
 // grid (enough for its larger axis); each domain keeps its own step state, so dt, time and cycle
 // advance per domain and a finished domain's blocks return at once.
+// Longest-first dispatch across the domains of a batch (both NULL when unused): block k of the
+// launch takes the launch's block order[k] and records the SM cycles it took in cost[order[k]].
+struct BatchOrder {
+    const uint32_t* order;
+    uint32_t* cost;
+};
+
 template <class T, int SCHEME, int PROJ, bool LAST>
 __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
-                                                          const int* __restrict__ offsets, int ndom, int pass)
+                                                          const int* __restrict__ offsets, int ndom, int pass,
+                                                          BatchOrder ord)
 {
-    const int b = blockIdx.x;
+    const int b = ord.order != nullptr ? (int)__ldg(&ord.order[blockIdx.x]) : (int)blockIdx.x;
+    const long long clock_start = clock64();
     int lo = 0, hi = ndom;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
@@ -667,6 +676,10 @@ __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_batch_kernel
     for (int w = threadIdx.x; w < (int)(sizeof(SweepArgs<T>) / 4); w += blockDim.x) dst[w] = src[w];
     __syncthreads();
     sweep_domain<T, SCHEME, PROJ, LAST>(sA, b - offsets[lo], offsets[lo + 1] - offsets[lo], pass);
+    if (ord.cost != nullptr) {
+        __syncthreads();
+        if (threadIdx.x == 0) ord.cost[b] = (uint32_t)min(clock64() - clock_start, (long long)0xFFFFFFFFu);
+    }
 }
 
 }  // namespace armon

@@ -14,9 +14,9 @@ cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool l
 }
 
 cudaError_t launch_sweep_batch(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks, int pass,
-                               int scheme, int proj, bool last, int block, cudaStream_t st)
+                               BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st)
 {
-    return launch_sweep_batch_t<float>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
+    return launch_sweep_batch_t<float>(doms, offsets, ndom, total_blocks, pass, ord, scheme, proj, last, block, st);
 }
 
 int sweep_blocks_per_sm_f32(int scheme, int proj, int block)

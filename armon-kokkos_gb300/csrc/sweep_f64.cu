@@ -12,9 +12,9 @@ cudaError_t launch_sweep(const SweepArgs<double>& a, int scheme, int proj, bool 
 }
 
 cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
-                               int scheme, int proj, bool last, int block, cudaStream_t st)
+                               BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st)
 {
-    return launch_sweep_batch_t<double>(doms, offsets, ndom, total_blocks, pass, scheme, proj, last, block, st);
+    return launch_sweep_batch_t<double>(doms, offsets, ndom, total_blocks, pass, ord, scheme, proj, last, block, st);
 }
 
 int sweep_blocks_per_sm_f64(int scheme, int proj, int block)

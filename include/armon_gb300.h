@@ -163,7 +163,8 @@ typedef struct armon_batch_opts {
     int32_t seg_len;          /* cells per thread along the sweep axis for every domain (0 = scheduled) */
     int64_t memory_budget;    /* bytes of domain state the batch may hold (0 = no limit) */
     int32_t waves;            /* scheduled segments: block waves per launch to aim for (0 = autotuned) */
-    int32_t reserved;
+    int32_t unit_order;       /* 0 (default): each pass launches the blocks of all domains longest
+                                 first, by the time each took in the previous cycle; -1: in index order */
 } armon_batch_opts;
 
 void armon_batch_opts_default(armon_batch_opts* o);

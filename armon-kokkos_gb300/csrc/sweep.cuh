@@ -76,6 +76,13 @@ constexpr int kSweepUnroll = ARMON_SWEEP_UNROLL;
 #endif
 template <class T> constexpr int sweep_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_SWEEP_MIN_BLOCKS; }
 
+// Load each cell's state one iteration ahead of its use: bit 0 for the FP64 pass, bit 1 for FP32.
+// The FP32 pass gains from it; the FP64 pass has no registers to spare for it.
+#ifndef ARMON_SWEEP_PREFETCH
+#define ARMON_SWEEP_PREFETCH 2
+#endif
+template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return ((ARMON_SWEEP_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
+
 namespace armon {
 
 template <class T>
@@ -521,25 +528,54 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         T s01{}, s12{}, s23{};               // W(j) + W(j+1)
         Adv<T> A0{}, A1{};
 
+        // position tt of the line -> the cell read there: itself (real, or an untouched ghost past the
+        // mirrored band: stale), or the mirror of a real cell (side 1: low side, 2: high side)
+        const auto source = [&](int tt, int& m, int& side) {
+            m = tt;
+            side = 0;
+            bool stale = false;
+            if (tt < 0) {
+                if (tt >= -sw) { m = -1 - tt; side = 1; } else stale = true;
+            } else if (tt >= n) {
+                if (tt < n + sw) { m = 2 * n - 1 - tt; side = 2; } else stale = true;
+            }
+            return stale;
+        };
+        // the state of the next position, loaded one iteration ahead so that the loads' latency
+        // overlaps an iteration's arithmetic (ARMON_SWEEP_PREFETCH), else at the top of its iteration
+        constexpr bool kPrefetch = sweep_prefetch<T>();
+        T next_rho{}, next_ua{}, next_uo{}, next_E{};
+        if constexpr (kPrefetch) {
+            int m, side;
+            source(t0, m, side);
+            const int64_t i = base + (int64_t)m * s;
+            next_rho = rho_in[i]; next_ua = ua_in[i]; next_uo = uo_in[i]; next_E = E_in[i];
+        }
+
 #pragma unroll kSweepUnroll
         for (int t = t0; t <= t1; ++t) {
             // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
             C0 = C1; C1 = C2;
             {
                 CellIn<T> c;
-                bool stale = false;
-                int m = t;
-                int side = 0;   // 1: mirrored from the low side, 2: from the high side
-                if (t < 0) {
-                    if (t >= -sw) { m = -1 - t; side = 1; } else stale = true;
-                } else if (t >= n) {
-                    if (t < n + sw) { m = 2 * n - 1 - t; side = 2; } else stale = true;
-                }
+                int m, side;
+                const bool stale = source(t, m, side);
                 const int64_t idx = base + (int64_t)m * s;
-                c.rho = rho_in[idx];
-                c.ua = ua_in[idx];
-                c.uo = uo_in[idx];
-                c.E = E_in[idx];
+                if constexpr (kPrefetch) {
+                    c.rho = next_rho;
+                    c.ua = next_ua;
+                    c.uo = next_uo;
+                    c.E = next_E;
+                    int m1, side1;
+                    source(min(t + 1, t1), m1, side1);
+                    const int64_t i1 = base + (int64_t)m1 * s;
+                    next_rho = rho_in[i1]; next_ua = ua_in[i1]; next_uo = uo_in[i1]; next_E = E_in[i1];
+                } else {
+                    c.rho = rho_in[idx];
+                    c.ua = ua_in[idx];
+                    c.uo = uo_in[idx];
+                    c.E = E_in[idx];
+                }
                 if (side) {
                     // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
                     if (g.f_unit) {

@@ -50,7 +50,7 @@ class Params(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("seg_len", C.c_int32),
                 ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("unit_order", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("split_pass", C.c_int32), ("reserved", C.c_int32)]
 
 
 class BatchOpts(C.Structure):
@@ -233,7 +233,7 @@ class Solver:
 
     def __init__(self, params: Params | Case, precision: int = 64, stream: int | None = None,
                  cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 0,
-                 unit_order: int = 0):
+                 unit_order: int = 0, split_pass: int = 0):
         L = lib()
         self.params = make_params(params) if isinstance(params, Case) else params
         o = SolverOpts()
@@ -244,6 +244,7 @@ class Solver:
         o.block_lines = block_lines
         o.materialize_eos = materialize_eos
         o.unit_order = unit_order
+        o.split_pass = split_pass
         self.opts = o
         h = C.c_void_p()
         check(L.armon_solver_create(C.byref(self.params), C.byref(o), C.c_void_p(stream or 0), C.byref(h)))

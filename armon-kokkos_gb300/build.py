@@ -32,6 +32,7 @@ EXTRA = os.environ.get("ARMON_NVCC_FLAGS", "").split()
 UNITS = [
     ("sweep_f64.cu", ["--fmad=false"]),
     ("sweep_f32.cu", ["--fmad=false"]),
+    ("sweep_split.cu", ["--fmad=false"]),
     ("abi_kernels.cu", ["--fmad=false"]),
     ("solver.cu", ["--fmad=false"]),
     ("batch.cu", ["--fmad=false"]),

@@ -16,6 +16,13 @@ cudaError_t launch_sweep(const SweepArgs<double>& a, int scheme, int proj, bool 
 cudaError_t launch_sweep(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
                          cudaStream_t st);
 
+// Split axis pass (sweep_split.cuh): the face half, then the cell half, on the same grid; a.faces
+// must hold 3 * a.face_stride values.
+cudaError_t launch_sweep_split(const SweepArgs<double>& a, int scheme, int proj, bool last, int grid, int block,
+                               cudaStream_t st);
+cudaError_t launch_sweep_split(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
+                               cudaStream_t st);
+
 // Fused axis pass over many domains (sweep_batch_kernel): doms / offsets are device arrays.
 cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
                                BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st);

@@ -57,6 +57,9 @@ struct armon_solver {
     uint32_t* d_order = nullptr;    // per axis: order_cap unit indices, then order_cap costs
     uint32_t* d_cost = nullptr;
     int order_cap = 0;
+    bool split = false;             // each pass as a face launch and a cell launch (sweep_split.cuh)
+    void* d_faces = nullptr;        // 3 * face_stride values
+    int64_t face_stride = 0;
 };
 
 namespace {
@@ -83,6 +86,10 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
                            s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[1]};
     s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, forced, b, s->d_state, s->d_partials,
                                  s->o.materialize_eos, a);
+    if (s->split) {
+        a.faces = static_cast<T*>(s->d_faces);
+        a.face_stride = s->face_stride;
+    }
 }
 
 int sync_state(armon_solver* s)
@@ -97,12 +104,15 @@ int axis_blocks(const armon_solver* s, int axis)
     return s->fp32 ? s->a32.geom[axis].blocks : s->a64.geom[axis].blocks;
 }
 
+// cost / order arrays: per axis for the (cell) pass, and per axis for the face half of split passes
+int order_arrays(const armon_solver* s) { return s->split ? 4 : 2; }
+
 // The next passes' unit order from the costs the last passes recorded.
 int launch_order(armon_solver* s)
 {
     if (!s->ordered) return ARMON_OK;
-    UnitCounts n{{axis_blocks(s, 0), axis_blocks(s, 1), 0, 0}};
-    order_units_kernel<<<2, 1024, 0, s->stream>>>(s->d_cost, s->d_order, s->order_cap, n);
+    UnitCounts n{{axis_blocks(s, 0), axis_blocks(s, 1), axis_blocks(s, 0), axis_blocks(s, 1)}};
+    order_units_kernel<<<order_arrays(s), 1024, 0, s->stream>>>(s->d_cost, s->d_order, s->order_cap, n);
     CUDA_TRY(cudaGetLastError());
     s->launches++;
     return ARMON_OK;
@@ -120,8 +130,8 @@ int prepare_order(armon_solver* s)
         cudaFree(s->d_cost);
         s->d_order = s->d_cost = nullptr;
         s->order_cap = 0;
-        cudaError_t e = cudaMalloc(&s->d_order, sizeof(uint32_t) * 2 * (size_t)need);
-        if (e == cudaSuccess) e = cudaMalloc(&s->d_cost, sizeof(uint32_t) * 2 * (size_t)need);
+        cudaError_t e = cudaMalloc(&s->d_order, sizeof(uint32_t) * order_arrays(s) * (size_t)need);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_cost, sizeof(uint32_t) * order_arrays(s) * (size_t)need);
         if (e != cudaSuccess) {
             set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
             return ARMON_ERR_NOMEM;
@@ -131,14 +141,34 @@ int prepare_order(armon_solver* s)
     for (int axis = 0; axis < 2; axis++) {
         uint32_t* o = s->d_order + (size_t)axis * s->order_cap;
         uint32_t* c = s->d_cost + (size_t)axis * s->order_cap;
-        if (s->fp32) { s->a32.geom[axis].order = o; s->a32.geom[axis].cost = c; }
-        else { s->a64.geom[axis].order = o; s->a64.geom[axis].cost = c; }
+        uint32_t* fo = s->split ? s->d_order + (size_t)(2 + axis) * s->order_cap : nullptr;
+        uint32_t* fc = s->split ? s->d_cost + (size_t)(2 + axis) * s->order_cap : nullptr;
+        if (s->fp32) {
+            s->a32.geom[axis].order = o; s->a32.geom[axis].cost = c;
+            s->a32.geom[axis].face_order = fo; s->a32.geom[axis].face_cost = fc;
+        } else {
+            s->a64.geom[axis].order = o; s->a64.geom[axis].cost = c;
+            s->a64.geom[axis].face_order = fo; s->a64.geom[axis].face_cost = fc;
+        }
     }
-    reset_order_kernel<<<std::max(1, std::min(s->sm_count * 4, (2 * s->order_cap + 255) / 256)), 256, 0, s->stream>>>(
-        s->d_order, s->d_cost, s->order_cap, 2);
+    const int total = order_arrays(s) * s->order_cap;
+    reset_order_kernel<<<std::max(1, std::min(s->sm_count * 4, (total + 255) / 256)), 256, 0, s->stream>>>(
+        s->d_order, s->d_cost, s->order_cap, order_arrays(s));
     CUDA_TRY(cudaGetLastError());
     s->launches++;
     return ARMON_OK;
+}
+
+cudaError_t launch_pass(armon_solver* s, int k, bool last)
+{
+    if (s->fp32) {
+        s->a32.pass = k;
+        return s->split ? launch_sweep_split(s->a32, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream)
+                        : launch_sweep(s->a32, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
+    }
+    s->a64.pass = k;
+    return s->split ? launch_sweep_split(s->a64, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream)
+                    : launch_sweep(s->a64, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
 }
 
 int enqueue_direct(armon_solver* s, int n_cycles)
@@ -147,15 +177,9 @@ int enqueue_direct(armon_solver* s, int n_cycles)
         for (int k = 0; k < s->npass; k++) {
             bool last = k == s->npass - 1;
             cudaError_t e;
-            if (s->fp32) {
-                s->a32.pass = k;
-                e = launch_sweep(s->a32, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
-            } else {
-                s->a64.pass = k;
-                e = launch_sweep(s->a64, s->p.scheme, s->p.projection, last, s->grid, s->block, s->stream);
-            }
+            e = launch_pass(s, k, last);
             if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-            s->launches++;
+            s->launches += s->split ? 2 : 1;
         }
         int rc = launch_order(s);
         if (rc != ARMON_OK) return rc;
@@ -187,7 +211,7 @@ int enqueue(armon_solver* s, int n_cycles)
         if (rc != ARMON_OK) return rc;
         while (n_cycles >= s->graph_cycles) {
             CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
-            s->launches += (int64_t)s->graph_cycles * (s->npass + (s->ordered ? 1 : 0));
+            s->launches += (int64_t)s->graph_cycles * (s->npass * (s->split ? 2 : 1) + (s->ordered ? 1 : 0));
             n_cycles -= s->graph_cycles;
         }
     }
@@ -241,16 +265,9 @@ std::mutex g_tilings_mu;
 
 int launch_pass0(armon_solver* s)
 {
-    cudaError_t e;
-    if (s->fp32) {
-        s->a32.pass = 0;
-        e = launch_sweep(s->a32, s->p.scheme, s->p.projection, false, s->grid, s->block, s->stream);
-    } else {
-        s->a64.pass = 0;
-        e = launch_sweep(s->a64, s->p.scheme, s->p.projection, false, s->grid, s->block, s->stream);
-    }
+    cudaError_t e = launch_pass(s, 0, false);
     if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-    s->launches++;
+    s->launches += s->split ? 2 : 1;
     return ARMON_OK;
 }
 
@@ -470,6 +487,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     s->elem = s->fp32 ? 4 : 8;
     s->block = s->o.block_lines > 0 ? s->o.block_lines : 128;
     s->ordered = s->o.unit_order >= 0;
+    s->split = s->o.split_pass > 0 || (s->o.split_pass == 0 && !s->fp32);
     if (s->block % 32 != 0 || s->block > 128) { delete s; set_error("block_lines must be a multiple of 32, at most 128"); return ARMON_ERR_PARAMS; }
     s->graph_cycles = s->o.cycles_per_graph;
     s->npass = passes_per_cycle(p->axis_splitting);
@@ -512,6 +530,10 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     if (e == cudaSuccess) e = cudaMalloc(&s->d_partials, sizeof(double) * 2 * (size_t)pblocks);
     s->partials_cap = pblocks;
     if (e == cudaSuccess) e = cudaMalloc(&s->d_cons, sizeof(double) * (2 * (size_t)s->cons_grid + 2));
+    if (e == cudaSuccess && s->split) {
+        s->face_stride = std::max((int64_t)(p->nx + 5) * p->ny, (int64_t)(p->ny + 5) * p->nx);
+        e = cudaMalloc(&s->d_faces, 3 * (size_t)s->face_stride * s->elem);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
     std::memset(s->h_state, 0, sizeof(StepState));
@@ -545,6 +567,7 @@ void armon_solver_destroy(armon_solver* s)
     if (s->d_partials) cudaFree(s->d_partials);
     if (s->d_cons) cudaFree(s->d_cons);
     if (s->stage) cudaFree(s->stage);
+    if (s->d_faces) cudaFree(s->d_faces);
     if (s->d_order) cudaFree(s->d_order);
     if (s->d_cost) cudaFree(s->d_cost);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);

@@ -158,6 +158,8 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, const 
         g.dx_log2 = g.dx_pow2 ? std::ilogb(double(g.dx)) : 0;
         g.order = nullptr;
         g.cost = nullptr;
+        g.face_order = nullptr;
+        g.face_cost = nullptr;
     }
     a.origin = (int64_t)p.nb_ghosts * p.row_length + p.nb_ghosts;
     a.sw = p.stencil_width;
@@ -173,6 +175,8 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, const 
     a.state = state;
     a.cfg = make_step_config(p);
     a.partials = partials;
+    a.faces = nullptr;
+    a.face_stride = 0;
     return std::max(a.geom[0].blocks, a.geom[1].blocks);
 }
 

@@ -76,6 +76,16 @@ constexpr int kSweepUnroll = ARMON_SWEEP_UNROLL;
 #endif
 template <class T> constexpr int sweep_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_SWEEP_MIN_BLOCKS; }
 
+// Blocks per SM the two halves of a split pass (sweep_split.cuh) must fit.
+#ifndef ARMON_FACES_MIN_BLOCKS
+#define ARMON_FACES_MIN_BLOCKS 3
+#endif
+#ifndef ARMON_CELLS_MIN_BLOCKS
+#define ARMON_CELLS_MIN_BLOCKS 3
+#endif
+template <class T> constexpr int sweep_faces_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_FACES_MIN_BLOCKS; }
+template <class T> constexpr int sweep_cells_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_CELLS_MIN_BLOCKS; }
+
 // Load each cell's state one iteration ahead of its use: bit 0 for the FP64 pass, bit 1 for FP32.
 // The FP32 pass gains from it; the FP64 pass has no registers to spare for it.
 #ifndef ARMON_SWEEP_PREFETCH
@@ -107,6 +117,8 @@ struct AxisGeom {
     // order[b] of the axis, and records the SM cycles that unit took in cost[unit].
     const uint32_t* order;
     uint32_t* cost;
+    const uint32_t* face_order;   // the same for the face half of a split pass (sweep_split.cuh)
+    uint32_t* face_cost;
 };
 
 template <class T>
@@ -125,6 +137,8 @@ struct SweepArgs {
     StepState* state;
     StepConfig cfg;
     double* partials;                 // 2 doubles per block (dt reduction)
+    T* faces;                         // split passes: u*, p*, p* u* per face (sweep_split.cuh)
+    int64_t face_stride;              // values per face array
 };
 
 // rc = rho c, rcu = rc ua, dm = rho dx: the products that the two faces of a cell both use
@@ -690,6 +704,8 @@ __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_kernel(const
 struct BatchOrder {
     const uint32_t* order;
     uint32_t* cost;
+    const uint32_t* face_order;   // the same for the face half of a split pass (sweep_split.cuh)
+    uint32_t* face_cost;
 };
 
 template <class T, int SCHEME, int PROJ, bool LAST>

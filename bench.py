@@ -286,7 +286,7 @@ def run_gpu(args) -> None:
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len,
-                 block_lines=args.block_lines)
+                 block_lines=args.block_lines, split_pass=args.split_pass)
     s.init_test()
     s.enqueue_cycles(W)
     torch.cuda.synchronize()
@@ -327,7 +327,7 @@ def run_gpu(args) -> None:
     case_e2e.nx, case_e2e.ny = nx, ny
     case_e2e.max_cycles = K
     se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
-                  seg_len=args.seg_len, block_lines=args.block_lines)
+                  seg_len=args.seg_len, block_lines=args.block_lines, split_pass=args.split_pass)
     se.init_test()
     outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
             for k in ("rho", "umat", "vmat", "Emat", "pmat")}
@@ -539,6 +539,9 @@ def main():
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
     ap.add_argument("--seg-len", type=int, default=0, help="cells per thread along the sweep axis (0 = automatic)")
     ap.add_argument("--block-lines", type=int, default=0, help="threads (lines) per block of the axis pass (0 = automatic)")
+    ap.add_argument("--split-pass", type=int, default=0, choices=[-1, 0, 1],
+                    help="1: each axis pass as a face launch and a cell launch; -1: one fused launch; "
+                         "0: the solver's default (split in FP64)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--accuracy-cycles", type=int, default=100,

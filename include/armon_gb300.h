@@ -91,7 +91,12 @@ typedef struct armon_solver_opts {
     int32_t unit_order;       /* 0 (default): each pass launches its blocks longest first, by the time
                                  each took in the previous cycle (results do not depend on it);
                                  -1: in index order */
-    int32_t reserved[2];
+    int32_t split_pass;       /* 0 (default): each FP64 axis pass runs as two launches (face
+                                 fluxes, then the cell update), each keeping fewer values per thread
+                                 than one fused launch, so that more warps fit on an SM; FP32 passes
+                                 stay fused.  1: split for either precision; -1: fused.  Results are
+                                 the same bits either way. */
+    int32_t reserved;
 } armon_solver_opts;
 
 void armon_solver_opts_default(armon_solver_opts* o);

@@ -234,3 +234,29 @@ def test_tiling_measured_on_developed_cycles_restores_the_state(precision):
     assert ta == tb and da == db
     for k in FIELDS:
         assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k
+
+
+SPLIT_CASES = [
+    dict(test="Sod_circ", scheme="GAD", projection="euler_2nd", splitting="Sequential"),
+    dict(test="Sod_circ", scheme="GAD", projection="euler", splitting="SequentialSym"),
+    dict(test="Sod", scheme="Godunov", projection="euler_2nd", splitting="Strang"),
+    dict(test="Sedov", scheme="Godunov", projection="euler", splitting="Sequential"),
+]
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("kw", SPLIT_CASES, ids=lambda k: f"{k['test']}-{k['scheme']}-{k['projection']}-{k['splitting']}")
+def test_split_pass_gives_the_fused_bits(kw, precision):
+    # the pass as two launches (face fluxes through a face buffer, then the cell update) computes
+    # the same operations on the same operands as the fused pass
+    case = A.Case(nghost=5, nx=200, ny=136, cfl=0.6, max_cycles=30, max_time=1e9, **kw)
+    out = []
+    for split in (-1, 1):
+        s, p, status = run_solver(case, precision=precision, split_pass=split, seg_len=40)
+        with s:
+            assert status == 0 and p.cycle == 30
+            out.append(({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt))
+    (a, ta, da), (b, tb, db) = out
+    assert ta == tb and da == db
+    for k in FIELDS:
+        assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k

@@ -52,8 +52,20 @@ struct Dom {
     void* arr[11] = {};           // set 0 (rho umat vmat Emat), set 1 (same), pmat cmat gmat
     double* partials = nullptr;
     int64_t npartials = 0;        // pairs
+    void* faces = nullptr;        // split passes: 3 face arrays of face_values(p) values
     int seg_len = 0;
 };
+
+// values per face array of a split pass (sweep_split.cuh): the larger axis's (n + 5) * nlines
+int64_t face_values(const armon_params& p)
+{
+    return std::max((int64_t)(p.nx + 5) * p.ny, (int64_t)(p.ny + 5) * p.nx);
+}
+
+// FP64 batches run split passes (face launch, cell launch) unless told otherwise
+bool split_default(int32_t precision) { return precision != 32; }
+
+
 
 int64_t partial_pairs(const armon_params& p, int block)
 {
@@ -62,6 +74,12 @@ int64_t partial_pairs(const armon_params& p, int block)
     int64_t bx = (int64_t)std::max(1, (p.ny + block - 1) / block) * std::max(1, p.nx / 16 + 1);
     int64_t by = (int64_t)std::max(1, (p.nx + block - 1) / block) * std::max(1, p.ny / 16 + 1);
     return std::max<int64_t>(std::max(bx, by), 152 * 4);
+}
+
+int64_t domain_bytes(const armon_params& p, size_t elem, bool split)
+{
+    return (int64_t)(11 * align256((size_t)p.nb_cells * elem) + align256(16 * (size_t)partial_pairs(p, 32)) +
+                     (split ? 3 * align256((size_t)face_values(p) * elem) : 0));
 }
 
 }  // namespace
@@ -90,9 +108,10 @@ struct armon_batch {
     cudaGraphExec_t graph = nullptr;
     int64_t bytes = 0;
     int64_t launches = 0;
+    bool split = true;            // passes as a face launch and a cell launch (sweep_split.cuh)
     bool ordered = true;          // longest-first dispatch of each pass's blocks
-    uint32_t* d_order = nullptr;  // npass arrays of order_cap block indices
-    uint32_t* d_cost = nullptr;   // npass arrays of order_cap costs
+    uint32_t* d_order = nullptr;  // per pass (and per half of a split pass) order_cap block indices
+    uint32_t* d_cost = nullptr;   // the same for the costs
     int order_cap = 0;
 };
 
@@ -186,6 +205,9 @@ std::vector<std::array<int, 2>> schedule_segments(const armon_batch* b)
     return seg;
 }
 
+// order / cost arrays: one per pass of a cycle, and one more per pass for the face halves
+int order_arrays(const armon_batch* b) { return b->npass * (b->split ? 2 : 1); }
+
 template <class T>
 int rebuild_t(armon_batch* b)
 {
@@ -193,7 +215,8 @@ int rebuild_t(armon_batch* b)
     for (int i = 0; i < (int)b->doms.size(); i++)
         if (b->doms[i].used && !b->doms[i].done) b->table.push_back(i);
     if (b->blocks_per_sm == 0 && !b->table.empty())
-        b->blocks_per_sm = sweep_batch_blocks_per_sm(b->fp32, b->scheme, b->proj, b->o.block_lines);
+        b->blocks_per_sm = b->split ? sweep_batch_split_blocks_per_sm(b->fp32, b->scheme, b->proj, b->o.block_lines)
+                                    : sweep_batch_blocks_per_sm(b->fp32, b->scheme, b->proj, b->o.block_lines);
     const std::vector<std::array<int, 2>> sched = schedule_segments(b);
     std::vector<SweepArgs<T>> args(b->table.size());
     std::vector<int> offsets(b->table.size() + 1, 0);
@@ -203,6 +226,10 @@ int rebuild_t(armon_batch* b)
         const int forced[2] = {fixed > 0 ? fixed : sched[k][0], fixed > 0 ? fixed : sched[k][1]};
         int nb = make_sweep_args<T>(d.p, b->npass, b->o.block_lines, b->sm_count, forced, buffers<T>(d),
                                     b->d_states + b->table[k], d.partials, 0, args[k]);
+        if (b->split) {
+            args[k].faces = static_cast<T*>(d.faces);
+            args[k].face_stride = face_values(d.p);
+        }
         if (nb > d.npartials) { set_error("domain needs more partial slots than allotted"); return ARMON_ERR_STATE; }
         offsets[k + 1] = offsets[k] + nb;
     }
@@ -220,9 +247,9 @@ int rebuild_t(armon_batch* b)
             CUDA_TRY(cudaMalloc(&b->d_cost, sizeof(uint32_t) * kMaxOrderArrays * (size_t)cap));
             b->order_cap = cap;
         }
-        const int total = b->order_cap * b->npass;
+        const int total = b->order_cap * order_arrays(b);
         reset_order_kernel<<<std::max(1, std::min(b->sm_count * 4, (total + 255) / 256)), 256, 0, b->stream>>>(
-            b->d_order, b->d_cost, b->order_cap, b->npass);
+            b->d_order, b->d_cost, b->order_cap, order_arrays(b));
         CUDA_TRY(cudaGetLastError());
         b->launches++;
     }
@@ -299,22 +326,33 @@ int enqueue_direct(armon_batch* b, int n)
     for (int c = 0; c < n; c++) {
         for (int k = 0; k < b->npass; k++) {
             bool last = k == b->npass - 1;
-            BatchOrder ord{nullptr, nullptr};
+            BatchOrder ord{nullptr, nullptr}, ford{nullptr, nullptr};
             if (b->ordered) {
                 ord.order = b->d_order + (size_t)k * b->order_cap;
                 ord.cost = b->d_cost + (size_t)k * b->order_cap;
+                if (b->split) {
+                    ford.order = b->d_order + (size_t)(b->npass + k) * b->order_cap;
+                    ford.cost = b->d_cost + (size_t)(b->npass + k) * b->order_cap;
+                }
             }
-            cudaError_t e = b->fp32
-                ? launch_sweep_batch((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks, k, ord,
-                                     b->scheme, b->proj, last, b->o.block_lines, b->stream)
-                : launch_sweep_batch((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks, k, ord,
-                                     b->scheme, b->proj, last, b->o.block_lines, b->stream);
+            cudaError_t e;
+            if (b->split)
+                e = b->fp32 ? launch_sweep_batch_split((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks,
+                                                       k, ford, ord, b->scheme, b->proj, last, b->o.block_lines, b->stream)
+                            : launch_sweep_batch_split((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks,
+                                                       k, ford, ord, b->scheme, b->proj, last, b->o.block_lines, b->stream);
+            else
+                e = b->fp32 ? launch_sweep_batch((const SweepArgs<float>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                                                 ord, b->scheme, b->proj, last, b->o.block_lines, b->stream)
+                            : launch_sweep_batch((const SweepArgs<double>*)b->d_args, b->d_offsets, nd, b->total_blocks, k,
+                                                 ord, b->scheme, b->proj, last, b->o.block_lines, b->stream);
             if (e != cudaSuccess) return cuda_fail(e, "batch sweep launch");
-            b->launches++;
+            b->launches += b->split ? 2 : 1;
         }
         if (b->ordered) {
-            UnitCounts counts{{b->total_blocks, b->total_blocks, b->total_blocks, b->total_blocks}};
-            order_units_kernel<<<b->npass, 1024, 0, b->stream>>>(b->d_cost, b->d_order, b->order_cap, counts);
+            UnitCounts counts;
+            for (int a = 0; a < kMaxOrderArrays; a++) counts.n[a] = b->total_blocks;
+            order_units_kernel<<<order_arrays(b), 1024, 0, b->stream>>>(b->d_cost, b->d_order, b->order_cap, counts);
             CUDA_TRY(cudaGetLastError());
             b->launches++;
         }
@@ -359,7 +397,7 @@ int enqueue(armon_batch* b, int n)
                 b->tune.launched = true;
                 b->tune.work = double(table_cells(b)) * gc;
             }
-            b->launches += (int64_t)gc * (b->npass + (b->ordered ? 1 : 0));
+            b->launches += (int64_t)gc * (b->npass * (b->split ? 2 : 1) + (b->ordered ? 1 : 0));
             n -= gc;
         }
     }
@@ -400,8 +438,7 @@ void armon_batch_opts_default(armon_batch_opts* o)
 
 int64_t armon_batch_domain_bytes(const armon_params* p, int32_t precision)
 {
-    size_t elem = precision == 32 ? 4 : 8;
-    return (int64_t)(11 * align256((size_t)p->nb_cells * elem) + align256(16 * (size_t)partial_pairs(*p, 32)));
+    return domain_bytes(*p, precision == 32 ? 4 : 8, split_default(precision));
 }
 
 int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch** out)
@@ -419,6 +456,7 @@ int armon_batch_create(const armon_batch_opts* opts, void* stream, armon_batch**
     b->fp32 = b->o.precision == 32;
     b->elem = b->fp32 ? 4 : 8;
     b->ordered = b->o.unit_order >= 0;
+    b->split = b->o.split_pass > 0 || (b->o.split_pass == 0 && split_default(b->o.precision));
     if (b->o.waves > 0) b->waves = b->o.waves;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -499,7 +537,7 @@ int add_domain(armon_batch* b, const armon_params* p, const double* const init[4
         set_error("all domains of a batch share scheme, projection and axis splitting");
         return ARMON_ERR_PARAMS;
     }
-    int64_t need = armon_batch_domain_bytes(p, b->o.precision);
+    int64_t need = domain_bytes(*p, b->elem, b->split);
     if (b->o.memory_budget > 0 && b->bytes + need > b->o.memory_budget) {
         set_error("the batch's memory budget would be exceeded");
         return ARMON_ERR_NOMEM;
@@ -522,6 +560,7 @@ int add_domain(armon_batch* b, const armon_params* p, const double* const init[4
     for (int k = 0; k < 11; k++) d.arr[k] = base + k * arr_bytes;
     d.partials = (double*)(base + 11 * arr_bytes);
     d.npartials = partial_pairs(*p, 32);
+    if (b->split) d.faces = base + 11 * arr_bytes + align256(16 * (size_t)d.npartials);
     b->doms[slot] = d;
     b->doms[slot].used = true;
     b->bytes += need;

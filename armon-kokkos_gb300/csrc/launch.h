@@ -23,6 +23,17 @@ cudaError_t launch_sweep_split(const SweepArgs<double>& a, int scheme, int proj,
 cudaError_t launch_sweep_split(const SweepArgs<float>& a, int scheme, int proj, bool last, int grid, int block,
                                cudaStream_t st);
 
+// Split axis pass over many domains: the face half with order `faces`, then the cell half with
+// order `cells`; each domain's arguments carry its face buffer.
+cudaError_t launch_sweep_batch_split(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks,
+                                     int pass, BatchOrder faces, BatchOrder cells, int scheme, int proj, bool last,
+                                     int block, cudaStream_t st);
+cudaError_t launch_sweep_batch_split(const SweepArgs<float>* doms, const int* offsets, int ndom, int total_blocks,
+                                     int pass, BatchOrder faces, BatchOrder cells, int scheme, int proj, bool last,
+                                     int block, cudaStream_t st);
+// Blocks of the split batch pass's cell half resident on one SM.
+int sweep_batch_split_blocks_per_sm(bool fp32, int scheme, int proj, int block);
+
 // Fused axis pass over many domains (sweep_batch_kernel): doms / offsets are device arrays.
 cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,
                                BatchOrder ord, int scheme, int proj, bool last, int block, cudaStream_t st);

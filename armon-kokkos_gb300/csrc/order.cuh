@@ -13,7 +13,7 @@
 namespace armon {
 
 constexpr int kOrderClasses = 64;
-constexpr int kMaxOrderArrays = 4;
+constexpr int kMaxOrderArrays = 6;
 
 struct UnitCounts {
     int n[kMaxOrderArrays];   // units of cost / order array k (block k of the kernel)

@@ -708,6 +708,33 @@ struct BatchOrder {
     uint32_t* face_cost;
 };
 
+// The domain of launch block b (domain d owns blocks [offsets[d], offsets[d+1])), its arguments
+// copied into shared memory: read once, and not aliased by the stores.
+template <class T>
+__device__ __forceinline__ int batch_domain(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets,
+                                            int ndom, int b, SweepArgs<T>& sA)
+{
+    int lo = 0, hi = ndom;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (offsets[mid] <= b) lo = mid; else hi = mid;
+    }
+    static_assert(sizeof(SweepArgs<T>) % 4 == 0, "word copy");
+    const int* src = reinterpret_cast<const int*>(&doms[lo]);
+    int* dst = reinterpret_cast<int*>(&sA);
+    for (int w = threadIdx.x; w < (int)(sizeof(SweepArgs<T>) / 4); w += blockDim.x) dst[w] = src[w];
+    __syncthreads();
+    return lo;
+}
+
+__device__ __forceinline__ void record_cost(const BatchOrder& ord, int b, long long clock_start)
+{
+    if (ord.cost != nullptr) {
+        __syncthreads();
+        if (threadIdx.x == 0) ord.cost[b] = (uint32_t)min(clock64() - clock_start, (long long)0xFFFFFFFFu);
+    }
+}
+
 template <class T, int SCHEME, int PROJ, bool LAST>
 __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_batch_kernel(const SweepArgs<T>* __restrict__ doms,
                                                           const int* __restrict__ offsets, int ndom, int pass,
@@ -715,23 +742,10 @@ __global__ void __launch_bounds__(128, sweep_min_blocks<T>()) sweep_batch_kernel
 {
     const int b = ord.order != nullptr ? (int)__ldg(&ord.order[blockIdx.x]) : (int)blockIdx.x;
     const long long clock_start = clock64();
-    int lo = 0, hi = ndom;
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (offsets[mid] <= b) lo = mid; else hi = mid;
-    }
-    // the block's domain arguments in shared memory: read once, and not aliased by the stores
     __shared__ __align__(16) SweepArgs<T> sA;
-    static_assert(sizeof(SweepArgs<T>) % 4 == 0, "word copy");
-    const int* src = reinterpret_cast<const int*>(&doms[lo]);
-    int* dst = reinterpret_cast<int*>(&sA);
-    for (int w = threadIdx.x; w < (int)(sizeof(SweepArgs<T>) / 4); w += blockDim.x) dst[w] = src[w];
-    __syncthreads();
+    const int lo = batch_domain(doms, offsets, ndom, b, sA);
     sweep_domain<T, SCHEME, PROJ, LAST>(sA, b - offsets[lo], offsets[lo + 1] - offsets[lo], pass);
-    if (ord.cost != nullptr) {
-        __syncthreads();
-        if (threadIdx.x == 0) ord.cost[b] = (uint32_t)min(clock64() - clock_start, (long long)0xFFFFFFFFu);
-    }
+    record_cost(ord, b, clock_start);
 }
 
 }  // namespace armon

@@ -301,4 +301,31 @@ __global__ void __launch_bounds__(128, sweep_cells_min_blocks<T>()) sweep_cells_
     sweep_cells<T, SCHEME, PROJ, LAST>(A, blockIdx.x, gridDim.x, A.pass);
 }
 
+// Many domains in one launch (sweep_batch_kernel's layout), each half on its own.
+template <class T, int SCHEME, bool LAST>
+__global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>())
+    sweep_batch_faces_kernel(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets, int ndom, int pass,
+                             BatchOrder ord)
+{
+    const int b = ord.order != nullptr ? (int)__ldg(&ord.order[blockIdx.x]) : (int)blockIdx.x;
+    const long long clock_start = clock64();
+    __shared__ __align__(16) SweepArgs<T> sA;
+    const int lo = batch_domain(doms, offsets, ndom, b, sA);
+    sweep_faces<T, SCHEME, LAST>(sA, b - offsets[lo], pass);
+    record_cost(ord, b, clock_start);
+}
+
+template <class T, int SCHEME, int PROJ, bool LAST>
+__global__ void __launch_bounds__(128, sweep_cells_min_blocks<T>())
+    sweep_batch_cells_kernel(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets, int ndom, int pass,
+                             BatchOrder ord)
+{
+    const int b = ord.order != nullptr ? (int)__ldg(&ord.order[blockIdx.x]) : (int)blockIdx.x;
+    const long long clock_start = clock64();
+    __shared__ __align__(16) SweepArgs<T> sA;
+    const int lo = batch_domain(doms, offsets, ndom, b, sA);
+    sweep_cells<T, SCHEME, PROJ, LAST>(sA, b - offsets[lo], offsets[lo + 1] - offsets[lo], pass);
+    record_cost(ord, b, clock_start);
+}
+
 }  // namespace armon

@@ -170,6 +170,10 @@ typedef struct armon_batch_opts {
     int32_t waves;            /* scheduled segments: block waves per launch to aim for (0 = autotuned) */
     int32_t unit_order;       /* 0 (default): each pass launches the blocks of all domains longest
                                  first, by the time each took in the previous cycle; -1: in index order */
+    int32_t split_pass;       /* as armon_solver_opts.split_pass: 0 (default) split FP64 passes into a
+                                 face launch and a cell launch (each domain then holds a face buffer,
+                                 counted by armon_batch_domain_bytes); 1: split; -1: fused */
+    int32_t reserved;
 } armon_batch_opts;
 
 void armon_batch_opts_default(armon_batch_opts* o);

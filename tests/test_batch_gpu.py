@@ -164,3 +164,19 @@ def test_late_joiners_with_parity_dependent_axes_match_solo(splitting):
                 got = A.real_cells(b.params[i], b.download(i, k))
                 assert np.array_equal(got.view(np.int64), ref[k].view(np.int64)), (splitting, k)
 
+
+
+def test_split_and_fused_batch_passes_agree_bitwise():
+    # the batch's passes as face + cell launches (the FP64 default) and as one fused launch
+    specs = small_domains(10, seed=23, sides=(24, 40, 64, 96, 130))
+    out = []
+    for split in (1, -1):
+        with A.Batch(cycles_per_graph=4, split_pass=split) as b:
+            ids = [b.add(s.params(), s.initial_state()) for s in specs]
+            assert b.run() == 0
+            out.append([(b.state(i)[0].cycle, b.state(i)[0].time,
+                         {k: b.download(i, k) for k in FIELDS}) for i in ids])
+    for (ca, ta, fa), (cb, tb, fb) in zip(*out):
+        assert ca == cb and ta == tb
+        for k in FIELDS:
+            assert np.array_equal(fa[k].view(np.int64), fb[k].view(np.int64)), k

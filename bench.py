@@ -63,13 +63,14 @@ def profiled(key: str, precision: int = 64) -> float | None:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(key + r":\s*([0-9.eE+-]+)", txt)
+    m = re.search(r"(?m)^" + re.escape(key) + r":\s*([0-9.eE+-]+)", txt)
     return float(m.group(1)) if m else None
 
 
-def profiled_traffic(precision: int = 64) -> float | None:
-    """DRAM bytes per cell and sweep launch (scaled to the workload by the caller)."""
-    return profiled("traffic_bytes_per_cell_per_pass", precision)
+def profiled_traffic(precision: int = 64, prefix: str = "") -> float | None:
+    """DRAM bytes per cell and axis pass (scaled to the workload by the caller); prefix "fused_" /
+    "split_" selects the figure of the pass form that is not the precision's default."""
+    return profiled(prefix + "traffic_bytes_per_cell_per_pass", precision)
 
 
 class ClockSampler:
@@ -126,13 +127,13 @@ class ClockSampler:
                 "samples": len(rs), "power_w_median": statistics.median(float(r[3]) for r in rs)}
 
 
-def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None) -> dict | None:
-    """The FP64 pipe as the bound: FP64 operations per cell and launch (ncu's DADD + DMUL + DFMA
+def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None, prefix: str = "") -> dict | None:
+    """The FP64 pipe as the bound: FP64 operations per cell and axis pass (ncu's DADD + DMUL + DFMA
     counts, profiles/) over the pipe's peak, 2 per SM per cycle (ncu's peak_sustained) at the SM
     clock sampled during the timed region."""
     import torch
 
-    ops = profiled("fp64_ops_per_cell_per_pass")
+    ops = profiled(prefix + "fp64_ops_per_cell_per_pass")
     if not ops:
         return None
     sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -140,7 +141,7 @@ def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None) -> dict |
     peak = 2.0 * sms * mhz * 1e6
     achieved = ops * cells * 2 / s_per_cycle
     return {"bound": "fp64", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G FP64 op/s",
-            "frac": achieved / peak, "ops_per_cell_per_launch": ops,
+            "frac": achieved / peak, "ops_per_cell_per_pass": ops,
             "note": "divisions, square roots and compares run on the integer pipes (exact), so only "
                     "additions and multiplications count here"}
 
@@ -353,7 +354,13 @@ def run_gpu(args) -> None:
         t_launch = ms_max / 1e3 / (K * 2)
         bpc = BYTES_PER_CELL_UPDATE if prec == 64 else BYTES_PER_CELL_UPDATE // 2
         achieved = bpc / 2 * cells / t_launch / 1e9
-        tr = profiled_traffic(prec)
+        split = args.split_pass == 1 or (args.split_pass == 0 and prec == 64)
+        prefix = "" if split == (prec == 64) else ("fused_" if prec == 64 else "split_")
+        tr = profiled_traffic(prec, prefix)
+        tname = "double" if prec == 64 else "float"
+        kernel = ("armon::sweep_faces_kernel<%s,1,*> + armon::sweep_cells_kernel<%s,1,2,*> (one axis pass = a face "
+                  "launch and a cell launch)" % (tname, tname) if split else
+                  "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)" % tname)
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64" if prec == 64 else "f32", "data": "synthetic",
@@ -362,13 +369,12 @@ def run_gpu(args) -> None:
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_source": peak_kind,
                             "traffic": (tr * cells if tr else None),
-                            "kernel": "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)"
-                                      % ("double" if prec == 64 else "float"),
-                            "algorithmic_bytes_per_launch": bpc / 2 * cells,
+                            "kernel": kernel,
+                            "algorithmic_bytes_per_pass": bpc / 2 * cells,
                             "note": ("not HBM-bound: the FP64 pipe and integer latency bound the pass (fp64_roofline, profiles/)"
                                      if prec == 64 else
                                      "not HBM-bound: instruction latency bounds the pass (12 warps per SM; profiles/)")},
-               "fp64_roofline": fp64_roofline(cells, ms_max / 1e3 / K, clocks) if prec == 64 else None,
+               "fp64_roofline": fp64_roofline(cells, ms_max / 1e3 / K, clocks, prefix) if prec == 64 else None,
                "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
                        "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,
                        "host_arrays": "FP64 (converted to the solver's precision inside the call)",

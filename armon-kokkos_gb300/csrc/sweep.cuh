@@ -91,6 +91,11 @@ template <class T> constexpr int sweep_cells_min_blocks() { return sizeof(T) == 
 #ifndef ARMON_SWEEP_PREFETCH
 #define ARMON_SWEEP_PREFETCH 2
 #endif
+// The same for the cell half of a split pass (sweep_split.cuh).
+#ifndef ARMON_CELLS_PREFETCH
+#define ARMON_CELLS_PREFETCH 0
+#endif
+template <class T> __host__ __device__ constexpr bool cells_prefetch() { return ((ARMON_CELLS_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return ((ARMON_SWEEP_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 
 namespace armon {

@@ -216,26 +216,53 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
         Adv<T> d01{}, d12{}, d23{};
         T s01{}, s12{}, s23{};
         Adv<T> A0{}, A1{};
+        // face t and cell t - 1 of the next iteration, loaded one iteration ahead (ARMON_CELLS_PREFETCH)
+        constexpr bool kPrefetch = cells_prefetch<T>();
+        Flux<T> next_f{};
+        CellIn<T> next_c{};
+        if constexpr (kPrefetch) {
+            const int64_t fi = face_index(g, t0, P.line);
+            next_f.us = us_in[fi];
+            next_f.ps = ps_in[fi];
+            next_f.psus = psus_in[fi];
+        }
 
 #pragma unroll 1
         for (int t = t0; t <= t1; ++t) {
             // ---- flux of face t ----
             F1 = F2; F2 = F3; F3 = F4;
             {
-                const int64_t fi = face_index(g, t, P.line);
                 Flux<T> f;
-                f.us = us_in[fi];
-                f.ps = ps_in[fi];
-                f.psus = psus_in[fi];
+                if constexpr (kPrefetch) {
+                    f = next_f;
+                    const int64_t fi = face_index(g, min(t + 1, t1), P.line);
+                    next_f.us = us_in[fi];
+                    next_f.ps = ps_in[fi];
+                    next_f.psus = psus_in[fi];
+                } else {
+                    const int64_t fi = face_index(g, t, P.line);
+                    f.us = us_in[fi];
+                    f.ps = ps_in[fi];
+                    f.psus = psus_in[fi];
+                }
                 f.dtus = qmul<4>(dt, f.us);
                 F4 = f;
             }
             // ---- Lagrange update of cell j = t - 1 ----
-            if (t >= t0 + 1) {
-                CellIn<T> c;
+            CellIn<T> cj = next_c;
+            if constexpr (kPrefetch) {
+                // positions up to t1 - 1, the last cell the segment updates, stay inside the ghost band
                 int m;
                 int64_t idx;
-                load_position(g, n, sw, base, t - 1, rho_in, ua_in, uo_in, E_in, c, m, idx);
+                load_position(g, n, sw, base, min(t, t1 - 1), rho_in, ua_in, uo_in, E_in, next_c, m, idx);
+            }
+            if (t >= t0 + 1) {
+                CellIn<T> c = cj;
+                if constexpr (!kPrefetch) {
+                    int m;
+                    int64_t idx;
+                    load_position(g, n, sw, base, t - 1, rho_in, ua_in, uo_in, E_in, c, m, idx);
+                }
                 c.dm = mul_dx(c.rho, g);
                 c.c = T(0);
                 L1 = L2; L2 = L3;

@@ -81,3 +81,20 @@ def test_boundary_factors_match_oracle():
             fa(test, side, C.byref(a[0]), C.byref(a[1]))
             O.lib().o_boundary_factors(test, side, C.byref(o[0]), C.byref(o[1]))
             assert (a[0].value, a[1].value) == (o[0].value, o[1].value)
+
+
+def _align256(n):
+    return (n + 255) & ~255
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 64), (300, 128), (1024, 2048)])
+def test_batch_domain_bytes_count_the_face_buffer_in_fp64(nx, ny):
+    # a batch domain holds 11 state arrays and its dt partials; an FP64 domain (split passes by
+    # default) also holds three face arrays of max((nx + 5) ny, (ny + 5) nx) values
+    p = A.make_params(A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=nx, ny=ny))
+    f64, f32 = A.domain_bytes(p, 64), A.domain_bytes(p, 32)
+    arrays64, arrays32 = 11 * _align256(p.nb_cells * 8), 11 * _align256(p.nb_cells * 4)
+    faces64 = 3 * _align256(max((nx + 5) * ny, (ny + 5) * nx) * 8)
+    partials = f32 - arrays32
+    assert 0 < partials < 1 << 24 and partials % 256 == 0
+    assert f64 == arrays64 + partials + faces64

@@ -713,17 +713,24 @@ struct BatchOrder {
     uint32_t* face_cost;
 };
 
-// The domain of launch block b (domain d owns blocks [offsets[d], offsets[d+1])), its arguments
-// copied into shared memory: read once, and not aliased by the stores.
-template <class T>
-__device__ __forceinline__ int batch_domain(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets,
-                                            int ndom, int b, SweepArgs<T>& sA)
+// The domain of launch block b: domain d owns blocks [offsets[d], offsets[d+1]).
+__device__ __forceinline__ int batch_domain_index(const int* __restrict__ offsets, int ndom, int b)
 {
     int lo = 0, hi = ndom;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
         if (offsets[mid] <= b) lo = mid; else hi = mid;
     }
+    return lo;
+}
+
+// The same, with the domain's arguments copied into shared memory: read once, and not aliased by
+// the stores.
+template <class T>
+__device__ __forceinline__ int batch_domain(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets,
+                                            int ndom, int b, SweepArgs<T>& sA)
+{
+    const int lo = batch_domain_index(offsets, ndom, b);
     static_assert(sizeof(SweepArgs<T>) % 4 == 0, "word copy");
     const int* src = reinterpret_cast<const int*>(&doms[lo]);
     int* dst = reinterpret_cast<int*>(&sA);

@@ -9,7 +9,7 @@ namespace {
 template <class T, int S, int P, bool L>
 cudaError_t launch_split_one(const SweepArgs<T>& a, int grid, int block, cudaStream_t st)
 {
-    sweep_faces_kernel<T, S, L><<<grid, block, 0, st>>>(a);
+    sweep_faces_kernel<T, S, P, L><<<grid, block, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     sweep_cells_kernel<T, S, P, L><<<grid, block, 0, st>>>(a);
@@ -33,7 +33,7 @@ template <class T, int S, int P, bool L>
 cudaError_t launch_batch_split_one(const SweepArgs<T>* doms, const int* offsets, int ndom, int grid, int pass,
                                    BatchOrder faces, BatchOrder cells, int block, cudaStream_t st)
 {
-    sweep_batch_faces_kernel<T, S, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass, faces);
+    sweep_batch_faces_kernel<T, S, P, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass, faces);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     sweep_batch_cells_kernel<T, S, P, L><<<grid, block, 0, st>>>(doms, offsets, ndom, pass, cells);

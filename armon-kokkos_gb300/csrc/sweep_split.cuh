@@ -8,8 +8,12 @@
 //
 // Face buffer: three arrays (u*, p*, p* u*) of face_stride values; face f of line l (f in [-2, n+2])
 // at (f + 2) * nlines + l, so that the 32 lines of a warp touch 32 consecutive values in either
-// pass.  The face half of segment [a0, b0) writes the faces it owns, [a0, b0) plus [-2, 0) for the
-// first segment and [n, n + 2] for the last; the cell half of the segment reads [a0 - 2, b0 + 2].
+// pass.  The cell half of segment [a0, b0) reads faces [a0 - r, b0 + r], r = 2 for the second-order
+// projection and 1 for the first; the face half of the segment writes the faces it owns, [a0, b0)
+// plus [-r, 0) for the first segment and [n, n + r] for the last.  A face's flux reads cells f - 2
+// to f + 1 (GAD) or f - 1 to f (Godunov), so the face half reads positions -(r + 2) to n + r + 1
+// (GAD) or -(r + 1) to n + r: never more than the 2 + GAD + second-order ghosts the solver
+// requires.
 #pragma once
 
 #include "sweep.cuh"
@@ -79,10 +83,11 @@ __device__ __forceinline__ bool load_position(const AxisGeom<T>& g, int n, int s
 }
 
 // ---- the face half: EOS of the cells, Godunov state of each face, GAD (or Godunov) flux ----
-template <class T, int SCHEME, bool LAST>
+template <class T, int SCHEME, int PROJ, bool LAST>
 __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk, const int pass)
 {
     constexpr bool kGAD = SCHEME == 1;
+    constexpr int R = PROJ == 2 ? 2 : 1;   // the cell half reads faces a0 - R .. b0 + R
     const StepState st = *A.state;
     const CycleDt cd = cycle_time_step(st, A.cfg);
     if (!cd.run || cd.invalid) return;   // the cell half reports an invalid dt
@@ -106,7 +111,7 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         const int n = g.n, sw = A.sw;
         const int a0 = P.seg * g.seg_len;
         const int b0 = min(n, a0 + g.seg_len);
-        const int fs = a0 == 0 ? -2 : a0, fe = b0 == n ? n + 3 : b0;   // faces [fs, fe) are this segment's
+        const int fs = a0 == 0 ? -R : a0, fe = b0 == n ? n + R + 1 : b0;   // faces [fs, fe) are this segment's
         const int64_t base = A.origin + (int64_t)P.line * g.lstride;
         const int t0 = kGAD ? fs - 2 : fs - 1, t1 = kGAD ? fe : fe - 1;
         T* const us_out = A.faces;
@@ -316,10 +321,10 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
     }
 }
 
-template <class T, int SCHEME, bool LAST>
+template <class T, int SCHEME, int PROJ, bool LAST>
 __global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>()) sweep_faces_kernel(const SweepArgs<T> A)
 {
-    sweep_faces<T, SCHEME, LAST>(A, blockIdx.x, A.pass);
+    sweep_faces<T, SCHEME, PROJ, LAST>(A, blockIdx.x, A.pass);
 }
 
 template <class T, int SCHEME, int PROJ, bool LAST>
@@ -329,7 +334,7 @@ __global__ void __launch_bounds__(128, sweep_cells_min_blocks<T>()) sweep_cells_
 }
 
 // Many domains in one launch (sweep_batch_kernel's layout), each half on its own.
-template <class T, int SCHEME, bool LAST>
+template <class T, int SCHEME, int PROJ, bool LAST>
 __global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>())
     sweep_batch_faces_kernel(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets, int ndom, int pass,
                              BatchOrder ord)
@@ -338,7 +343,7 @@ __global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>())
     const long long clock_start = clock64();
     __shared__ __align__(16) SweepArgs<T> sA;
     const int lo = batch_domain(doms, offsets, ndom, b, sA);
-    sweep_faces<T, SCHEME, LAST>(sA, b - offsets[lo], pass);
+    sweep_faces<T, SCHEME, PROJ, LAST>(sA, b - offsets[lo], pass);
     record_cost(ord, b, clock_start);
 }
 

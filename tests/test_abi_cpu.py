@@ -98,3 +98,29 @@ def test_batch_domain_bytes_count_the_face_buffer_in_fp64(nx, ny):
     partials = f32 - arrays32
     assert 0 < partials < 1 << 24 and partials % 256 == 0
     assert f64 == arrays64 + partials + faces64
+
+
+@pytest.mark.parametrize("gad", [0, 1])
+@pytest.mark.parametrize("second_order", [0, 1])
+def test_split_pass_positions_stay_inside_the_required_ghosts(gad, second_order):
+    # the index ranges of csrc/sweep_split.cuh for a line of n cells cut into segments, against the
+    # ghost depth the solver requires (2 + GAD + second order); a restatement of the kernel's
+    # arithmetic, checked here before any GPU runs it
+    reach = 2 + gad + second_order
+    r = 2 if second_order else 1
+    for n, seg in ((16, 16), (40, 7), (100, 33), (5, 1)):
+        segments = [(a0, min(n, a0 + seg)) for a0 in range(0, n, seg)]
+        written, lo, hi = set(), 10**9, -10**9
+        for a0, b0 in segments:
+            fs = -r if a0 == 0 else a0
+            fe = n + r + 1 if b0 == n else b0
+            assert not written & set(range(fs, fe))                  # each face has one writer
+            written |= set(range(fs, fe))
+            t0, t1 = (fs - 2, fe) if gad else (fs - 1, fe - 1)       # the face half's positions
+            lo, hi = min(lo, t0), max(hi, t1)
+        for a0, b0 in segments:
+            t0, t1 = a0 - r, b0 + r                                  # the cell half's iterations
+            assert set(range(t0, t1 + 1)) <= written                 # face t of each iteration
+            lo, hi = min(lo, t0 - 1), max(hi, t1 - 1)                # cell t - 1 of each iteration
+        assert written == set(range(-r, n + r + 1)) and -2 <= -r and n + r <= n + 2   # n + 5 faces a line
+        assert -reach <= lo and hi <= n + reach - 1, (n, seg, lo, hi, reach)

@@ -241,6 +241,7 @@ SPLIT_CASES = [
     dict(test="Sod_circ", scheme="GAD", projection="euler", splitting="SequentialSym"),
     dict(test="Sod", scheme="Godunov", projection="euler_2nd", splitting="Strang"),
     dict(test="Sedov", scheme="Godunov", projection="euler", splitting="Sequential"),
+    dict(test="Sod_y", scheme="GAD", projection="euler", splitting="Sequential"),
 ]
 
 
@@ -249,7 +250,10 @@ SPLIT_CASES = [
 def test_split_pass_gives_the_fused_bits(kw, precision):
     # the pass as two launches (face fluxes through a face buffer, then the cell update) computes
     # the same operations on the same operands as the fused pass
-    case = A.Case(nghost=5, nx=200, ny=136, cfl=0.6, max_cycles=30, max_time=1e9, **kw)
+    # the fewest ghosts the solver accepts for the scheme (2 + GAD + second order), so that the face
+    # half's reads at the domain edges run right up to the end of the ghost band
+    nghost = 2 + (kw["scheme"] == "GAD") + (kw["projection"] == "euler_2nd")
+    case = A.Case(nghost=nghost, nx=200, ny=136, cfl=0.6, max_cycles=30, max_time=1e9, **kw)
     out = []
     for split in (-1, 1):
         s, p, status = run_solver(case, precision=precision, split_pass=split, seg_len=40)

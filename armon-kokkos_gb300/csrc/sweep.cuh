@@ -46,8 +46,15 @@
 // Stages whose FP64 products run on the integer pipes (sfp::mul), one bit per stage: 0 EOS,
 // 1 rho c and rho c u, 2 Godunov, 3 GAD, 4 face products, 5 Lagrange, 6 advection, 7 projection.
 // The FP64 pipe and the integer pipes then share the products; results are the same either way.
+// The mask applies to every kernel; the solver's split face half adds ARMON_FACES_SOFT_MUL: it
+// keeps the FP64 pipe ~82 % busy with 16 warps per SM to hide the longer integer chains, and
+// taking the GAD products off the pipe pays there (+2 %), while the batch and fused kernels,
+// with fewer registers to spare, measured slower with it.
 #ifndef ARMON_SOFT_MUL
 #define ARMON_SOFT_MUL 0
+#endif
+#ifndef ARMON_FACES_SOFT_MUL
+#define ARMON_FACES_SOFT_MUL 0x08
 #endif
 
 // Division sites that use the FP64 pipe's IEEE division instead of the integer-pipe one, one bit
@@ -192,11 +199,11 @@ __device__ __forceinline__ double qscale(double x, int k, double p2) { return AR
 __device__ __forceinline__ float qscale(float x, int, float p2) { return x * p2; }
 __device__ __forceinline__ double qsqrt(double x) { return ARMON_SOFT_FP64 ? sfp::sqrt(x) : ::sqrt(x); }
 __device__ __forceinline__ float qsqrt(float x) { return sqrtf(x); }
-template <int G> __device__ __forceinline__ double qmul(double a, double b)
+template <int G, int MASK = ARMON_SOFT_MUL> __device__ __forceinline__ double qmul(double a, double b)
 {
-    return (ARMON_SOFT_FP64 && ((ARMON_SOFT_MUL >> G) & 1)) ? sfp::mul(a, b) : a * b;
+    return (ARMON_SOFT_FP64 && (((ARMON_SOFT_MUL | MASK) >> G) & 1)) ? sfp::mul(a, b) : a * b;
 }
-template <int G> __device__ __forceinline__ float qmul(float a, float b) { return a * b; }
+template <int G, int MASK = ARMON_SOFT_MUL> __device__ __forceinline__ float qmul(float a, float b) { return a * b; }
 // Kokkos::min / Kokkos::max: (b < a) ? b : a and (a < b) ? b : a
 template <class T> __device__ __forceinline__ T qmin(T a, T b) { return qlt(b, a) ? b : a; }
 template <class T> __device__ __forceinline__ T qmax(T a, T b) { return qlt(a, b) ? b : a; }
@@ -292,7 +299,7 @@ __device__ __forceinline__ GadDiff<T> gad_diff(const God<T>& G, const CellIn<T>&
     return d;
 }
 
-template <class T>
+template <class T, int MULS = ARMON_SOFT_MUL>
 __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, const GadDiff<T>& D0,
                                        const GadDiff<T>& Dp1, T dm_l, T dm_r, int L, T dt)
 {
@@ -304,10 +311,10 @@ __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, 
     const T r_up = limited_ratio(L, Dm1.bu, D0.bu + T(1e-6));
     const T r_pp = limited_ratio(L, Dm1.bp, D0.bp + T(1e-6));
     T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
-    T theta = qhalf(1 - qmul<3>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
+    T theta = qhalf(1 - qmul<3, MULS>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
-    f.us = Gc.us + qmul<3>(theta, qmul<3>(r_up, D0.bu) - qmul<3>(r_um, D0.au));
-    f.ps = Gc.ps + qmul<3>(theta, qmul<3>(r_pp, D0.bp) - qmul<3>(r_pm, D0.ap));
+    f.us = Gc.us + qmul<3, MULS>(theta, qmul<3, MULS>(r_up, D0.bu) - qmul<3, MULS>(r_um, D0.au));
+    f.ps = Gc.ps + qmul<3, MULS>(theta, qmul<3, MULS>(r_pp, D0.bp) - qmul<3, MULS>(r_pm, D0.ap));
     return f;
 }
 

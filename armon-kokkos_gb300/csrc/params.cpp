@@ -101,7 +101,7 @@ void armon_params_init(armon_params* p)
     }
 }
 
-// Params::check, src/parameters.cpp:70-109 (the warnings do not change the verdict)
+// Params::check, src/parameters.cpp:70-109 (the warnings do not change the outcome)
 int armon_params_check(const armon_params* p)
 {
     if (p->projection == ARMON_PROJ_NONE) return 0;

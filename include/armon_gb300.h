@@ -38,7 +38,7 @@ enum {
     ARMON_ERR_INVALID_DT = 1,   /* a non-finite or non-positive time step (the reference exits) */
     ARMON_ERR_PARAMS = 2,       /* Params::check failed, or an argument is out of range */
     ARMON_ERR_CUDA = 3,         /* a CUDA call failed; see armon_last_error() */
-    ARMON_ERR_UNSUPPORTED = 4,  /* a combination this build does not implement */
+    ARMON_ERR_UNSUPPORTED = 4,  /* a combination the library does not implement */
     ARMON_ERR_NOMEM = 5,        /* device allocation failed or would exceed the budget */
     ARMON_ERR_STATE = 6         /* the device step state is inconsistent (e.g. a skipped cycle) */
 };

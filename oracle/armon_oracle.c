@@ -666,7 +666,7 @@ void o_params_init(o_params* p)
     o_update_axis(p, p->current_axis);
 }
 
-/* src/parameters.cpp:70-109 (errors only; the warnings do not change the verdict) */
+/* src/parameters.cpp:70-109 (errors only; the warnings do not change the outcome) */
 int o_params_check(const o_params* p)
 {
     if (p->projection == O_PROJ_NONE) return 0;

@@ -533,6 +533,14 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
     if (e == cudaSuccess && s->split) {
         s->face_stride = std::max((int64_t)(p->nx + 5) * p->ny, (int64_t)(p->ny + 5) * p->nx);
         e = cudaMalloc(&s->d_faces, 3 * (size_t)s->face_stride * s->elem);
+        if (e == cudaErrorMemoryAllocation && s->o.split_pass == 0) {
+            // the split pass is only the default here: run fused passes, which need no face buffer
+            cudaGetLastError();
+            s->d_faces = nullptr;
+            s->face_stride = 0;
+            s->split = false;
+            e = cudaSuccess;
+        }
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }

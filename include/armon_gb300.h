@@ -93,9 +93,10 @@ typedef struct armon_solver_opts {
                                  -1: in index order */
     int32_t split_pass;       /* 0 (default): each FP64 axis pass runs as two launches (face
                                  fluxes, then the cell update), each keeping fewer values per thread
-                                 than one fused launch, so that more warps fit on an SM; FP32 passes
-                                 stay fused.  1: split for either precision; -1: fused.  Results are
-                                 the same bits either way. */
+                                 than one fused launch, so that more warps fit on an SM (fused when
+                                 the face buffer, 3 x max((nx+5) ny, (ny+5) nx) values, cannot be
+                                 allocated); FP32 passes stay fused.  1: split for either precision;
+                                 -1: fused.  Results are the same bits either way. */
     int32_t reserved;
 } armon_solver_opts;
 

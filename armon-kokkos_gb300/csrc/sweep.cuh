@@ -92,6 +92,11 @@ template <class T> constexpr int sweep_min_blocks() { return sizeof(T) == 4 ? AR
 #endif
 template <class T> constexpr int sweep_faces_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_FACES_MIN_BLOCKS; }
 template <class T> constexpr int sweep_cells_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_CELLS_MIN_BLOCKS; }
+// the batch's cell half reads its arguments from shared memory and needs more registers for them
+#ifndef ARMON_BATCH_CELLS_MIN_BLOCKS
+#define ARMON_BATCH_CELLS_MIN_BLOCKS ARMON_CELLS_MIN_BLOCKS
+#endif
+template <class T> constexpr int sweep_batch_cells_min_blocks() { return sizeof(T) == 4 ? ARMON_SWEEP_MIN_BLOCKS_F32 : ARMON_BATCH_CELLS_MIN_BLOCKS; }
 
 // Load each cell's state one iteration ahead of its use: bit 0 for the FP64 pass, bit 1 for FP32.
 // The FP32 pass gains from it; the FP64 pass has no registers to spare for it.

@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>())
 }
 
 template <class T, int SCHEME, int PROJ, bool LAST>
-__global__ void __launch_bounds__(128, sweep_cells_min_blocks<T>())
+__global__ void __launch_bounds__(128, sweep_batch_cells_min_blocks<T>())
     sweep_batch_cells_kernel(const SweepArgs<T>* __restrict__ doms, const int* __restrict__ offsets, int ndom, int pass,
                              BatchOrder ord)
 {

@@ -308,10 +308,17 @@ int time_candidates(armon_solver* s, const std::vector<Tiling>& cand, int cycles
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
-    float best_ms = 1e30f;
-    *best = 0;
+    // On developed cycles the state keeps developing while the candidates run, so each is timed
+    // twice, the list forwards and then backwards, and the two times are summed: a cost that
+    // drifts linearly with the cycle then weighs the same on every candidate.
+    std::vector<float> total(cand.size(), 0.f);
+    std::vector<size_t> seq;
+    for (size_t i = 0; i < cand.size(); i++) seq.push_back(i);
+    if (cycles > 0)
+        for (size_t i = cand.size(); i-- > 0;) seq.push_back(i);
     int rc = ARMON_OK;
-    for (size_t i = 0; i < cand.size() && rc == ARMON_OK; i++) {
+    for (size_t q = 0; q < seq.size() && rc == ARMON_OK; q++) {
+        const size_t i = seq[q];
         set_tiling(s, cand[i]);
         rc = refill(s);
         if (rc == ARMON_OK) rc = ensure_partials(s);
@@ -326,10 +333,11 @@ int time_candidates(armon_solver* s, const std::vector<Tiling>& cand, int cycles
         if (rc == ARMON_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
         float ms = 0;
         if (rc == ARMON_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK && ms < best_ms) { best_ms = ms; *best = i; }
+        total[i] += ms;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    *best = size_t(std::min_element(total.begin(), total.end()) - total.begin());
     return rc;
 }
 
@@ -388,7 +396,7 @@ int tune_tiling(armon_solver* s)
     // On developed cycles when the device has room for a copy of the state, else on the pass of
     // cycle 0.  The measured cycles run past the caller's max_cycles / max_time if need be: the
     // copy is put back afterwards and the loop bounds with it.
-    const int need = kTuneWarmCycles + (int)cand.size() * (1 + kTuneCycles);
+    const int need = kTuneWarmCycles + 2 * (int)cand.size() * (1 + kTuneCycles);
     void* snap[7] = {};
     bool developed = true;
     const size_t bytes = (size_t)p.nb_cells * s->elem;

@@ -1,6 +1,7 @@
 // selftest.cu -- checks of the integer-pipe FP64 operations (softfp.cuh) against the FP64
 // instructions, on generated operands.  Exposed as armon_selftest_softfp for the test suite.
 #include <cstdint>
+#include <cstring>
 
 #include <cuda_runtime.h>
 
@@ -8,7 +9,7 @@
 
 namespace {
 
-__device__ __forceinline__ uint64_t mix(uint64_t x)
+__host__ __device__ __forceinline__ uint64_t mix(uint64_t x)
 {
     // splitmix64 finaliser
     x += 0x9E3779B97F4A7C15ull;
@@ -225,15 +226,95 @@ __global__ void quot_check(uint64_t seed, int64_t n, unsigned long long* out)
     }
 }
 
+
+// Operands for the addition check: every bit class, cancellations (|a| close to |b|, opposite
+// signs), exact ties (y's dropped part exactly half a unit), large exponent differences, overflow
+// and underflow ranges, zeros, and the solver's ranges.
+__host__ __device__ void add_operands(uint64_t seed, uint64_t i, uint64_t& ua, uint64_t& ub)
+{
+    using namespace armon::sfp;
+    const uint64_t r1 = mix(seed ^ (2 * i)), r2 = mix(seed ^ (2 * i + 1)), r3 = mix(r1 ^ r2);
+    const auto normal = [](uint64_t r, uint32_t lo, uint32_t span) {
+        return (r & ~kAbs) | ((uint64_t)(lo + (uint32_t)((r >> 53) % span)) << 52) | (r & kMant);
+    };
+    switch (r3 & 7) {
+    case 0: ua = r1; ub = r2; break;                                              // every class
+    case 1: {                                                                      // cancellation
+        ua = normal(r1, 1000, 48);
+        const uint64_t delta = (r2 >> ((r3 >> 8) % 64)) & 0xFFFFFull;
+        ub = (((ua & kAbs) + ((r3 & 16) ? delta : (uint64_t)0 - delta)) & kAbs) | (~ua & ~kAbs);
+        break;
+    }
+    case 2: {                                                                      // ties and near ties
+        ua = normal(r1, 900, 200);
+        const uint32_t d = 1 + (uint32_t)((r3 >> 8) % 60);
+        const uint64_t ea = (ua >> 52) & 0x7FF;
+        const uint64_t m = (r2 & kMant & ~((1ull << (d < 52 ? d : 52)) - 1)) | ((r3 >> 20) & 1 ? (1ull << (d - 1 < 52 ? d - 1 : 51)) : 0);
+        ub = (r2 & ~kAbs) | ((ea > d ? ea - d : 1) << 52) | (m & kMant);
+        break;
+    }
+    case 3: ua = normal(r1, 1, 2046); ub = normal(r2, 1, 2046); break;            // every exponent
+    case 4: ua = normal(r1, 2000, 46); ub = normal(r2, 2000, 46); break;          // overflow
+    case 5: ua = normal(r1, 1, 60); ub = normal(r2, 1, 60); break;                // underflow
+    case 6: ua = normal(r1, 1000, 48); ub = (r3 & 32) ? (r2 & ~kAbs) : normal(r2, 1000, 48); break;   // zeros
+    default: ua = normal(r1, 1003, 40); ub = normal(r2, 1003, 40); break;         // the solver's ranges
+    }
+}
+
+__global__ void add_check(uint64_t seed, int64_t n, unsigned long long* out)
+{
+    using namespace armon::sfp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t ua, ub;
+        add_operands(seed, (uint64_t)i, ua, ub);
+        const double a = from_bits(ua), b = from_bits(ub);
+        const double s = add(a, b), h = a + b;
+        if (!(bits(s) == bits(h) || (s != s && h != h)) && atomicAdd(&out[0], 1ull) == 0) {
+            out[2] = ua;
+            out[3] = ub;
+        }
+        bool ok;
+        add_bits(ua, ub, ok);
+        if (ok) atomicAdd(&out[1], 1ull);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+// add_bits on the host against the host's IEEE addition, on the operands of add_check:
+// out[0] = mismatches, out[1] = operand pairs on the integer path, out[2..3] = the first mismatch.
+int armon_selftest_add_host(uint64_t seed, int64_t n, uint64_t* out)
+{
+    out[0] = out[1] = out[2] = out[3] = 0;
+    for (int64_t i = 0; i < n; i++) {
+        uint64_t ua, ub;
+        add_operands(seed, (uint64_t)i, ua, ub);
+        bool ok;
+        const uint64_t r = armon::sfp::add_bits(ua, ub, ok);
+        if (!ok) continue;
+        out[1]++;
+        double a, b, h;
+        std::memcpy(&a, &ua, 8);
+        std::memcpy(&b, &ub, 8);
+        h = a + b;
+        uint64_t uh;
+        std::memcpy(&uh, &h, 8);
+        if (uh != r && out[0]++ == 0) {
+            out[2] = ua;
+            out[3] = ub;
+        }
+    }
+    return 0;
+}
 
 // mode 0..6 (see operands) checks sfp::div against the hardware quotient; mode 100 checks lt,
 // gt0 and neg_if against the IEEE comparisons; mode 101 checks scale, half and twice against the
 // FP64 multiply by the power of two (out[3] = the exponent k of the first mismatch); mode 102
 // checks sqrt and absval against the hardware square root and fabs (out[3] = the soft root);
-// mode 103 checks mul against the FP64 multiply; mode 104 checks the division's quotient
+// mode 103 checks mul against the FP64 multiply; mode 105 checks add against the FP64 addition;
+// mode 104 checks the division's quotient
 // estimate against 128-bit arithmetic (out[2..3] = ma, mb of the first miss).  out[0] = mismatches, out[1] = fast-path operand
 // pairs, out[2..3] = the bits of the first mismatching operands.  Returns a cudaError_t.
 int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_host)
@@ -247,6 +328,7 @@ int armon_selftest_softfp(uint64_t seed, int64_t n, int32_t mode, uint64_t* out_
     else if (mode == 102) sqrt_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 103) mul_check<<<152 * 16, 256>>>(seed, n, out);
     else if (mode == 104) quot_check<<<152 * 16, 256>>>(seed, n, out);
+    else if (mode == 105) add_check<<<152 * 16, 256>>>(seed, n, out);
     else div_check<<<152 * 16, 256>>>(mode, seed, n, out);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpy(out_host, out, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);

@@ -13,6 +13,8 @@
 //   absval(x)     |x|
 //   div(a, b)     the correctly rounded quotient (round to nearest, ties to even)
 //   sqrt(x)       the correctly rounded square root
+//   mul(a, b)     the correctly rounded product
+//   add(a, b)     the correctly rounded sum (add_bits: the same on bit patterns, host or device)
 //
 // Division (my own construction from the arithmetic, not a library's sequence).  With
 // significands ma, mb in [2^52, 2^53) and ma doubled when ma < mb, the result significand is
@@ -247,6 +249,81 @@ __device__ __forceinline__ double mul(double a, double b)
         ((ua << 1) == 0 && (ub << 1) == 0))
         return from_bits(sign);                                  // +-0 * normal or zero
     return a * b;
+}
+
+// Addition (my own construction).  For normal operands, x the one of larger magnitude and y the
+// other, the significands are placed at bits 62..10 of 64-bit words (ten guard bits) and y's is
+// shifted right by the exponent difference d, what falls off kept as a sticky bit.  Same signs:
+// the sum, renormalised by one place when it carries into bit 63.  Opposite signs: the
+// difference, minus one more unit when the sticky bit is set (the true value then lies strictly
+// between that integer and the next), renormalised to bit 62; a sticky bit only arises for
+// d >= 11, where at most one place of renormalisation is needed and the guard bits still decide
+// the rounding.  Round to nearest, ties to even, on the ten guard bits and the sticky bit.  x - x
+// gives +0; a zero operand gives the other operand (-0 only for -0 + -0); subnormal, infinite and
+// NaN operands, subnormal results and overflow take the FP64 addition (ok = false).
+__host__ __device__ __forceinline__ int clz64(uint64_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return __builtin_clzll(x);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint64_t add_bits(uint64_t ua, uint64_t ub, bool& ok)
+{
+    const uint32_t ea = (uint32_t)(ua >> 52) & 0x7FFu, eb = (uint32_t)(ub >> 52) & 0x7FFu;
+    ok = false;
+    if (!((ea - 1u) < 2046u && (eb - 1u) < 2046u)) {
+        const bool za = (ua << 1) == 0, zb = (ub << 1) == 0;
+        if (za && zb) { ok = true; return ua & ub; }
+        if (zb && (ea - 1u) < 2046u) { ok = true; return ua; }
+        if (za && (eb - 1u) < 2046u) { ok = true; return ub; }
+        return 0;
+    }
+    const bool swap = (ub & kAbs) > (ua & kAbs);
+    const uint64_t ux = swap ? ub : ua, uy = swap ? ua : ub;
+    const uint32_t d = swap ? eb - ea : ea - eb;
+    int e = (int)(swap ? eb : ea);
+    const uint64_t mx = ((ux & kMant) | kHidden) << 10;     // [2^62, 2^63)
+    const uint64_t my = ((uy & kMant) | kHidden) << 10;
+    uint64_t ys;
+    bool sticky;
+    if (d >= 64) {
+        ys = 0;
+        sticky = true;
+    } else {
+        ys = my >> d;
+        sticky = d != 0 && (my << (64 - d)) != 0;
+    }
+    uint64_t sum;
+    if (((ux ^ uy) >> 63) == 0) {
+        sum = mx + ys;                                       // < 2^64
+        if (sum >> 63) {
+            sticky = sticky || (sum & 1) != 0;
+            sum >>= 1;
+            e += 1;
+        }
+    } else {
+        sum = mx - ys - (sticky ? 1u : 0u);
+        if (sum == 0) { ok = true; return 0; }               // x - x = +0
+        const int sh = clz64(sum) - 1;
+        sum <<= sh;
+        e -= sh;
+        if (e < 1) return 0;                                 // subnormal result
+    }
+    if (e > 2046) return 0;                                  // overflow
+    const uint64_t m = sum >> 10, rem = sum & 0x3FFu;
+    const bool up = rem > 0x200u || (rem == 0x200u && (sticky || (m & 1)));
+    ok = true;
+    return (ux & ~kAbs) + ((uint64_t)(e - 1) << 52) + m + (up ? 1u : 0u);
+}
+
+__device__ __forceinline__ double add(double a, double b)
+{
+    bool ok;
+    const uint64_t r = add_bits(bits(a), bits(b), ok);
+    return ok ? from_bits(r) : a + b;
 }
 
 // Square root (my own construction, in the manner of the division above).  A positive normal

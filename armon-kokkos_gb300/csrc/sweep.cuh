@@ -56,6 +56,11 @@
 #ifndef ARMON_FACES_SOFT_MUL
 #define ARMON_FACES_SOFT_MUL 0x08
 #endif
+// The same for additions and subtractions (sfp::add), by stage: 2 Godunov, 3 GAD.  Only the
+// solver's split face half takes them (ARMON_FACES_SOFT_ADD).
+#ifndef ARMON_FACES_SOFT_ADD
+#define ARMON_FACES_SOFT_ADD 0
+#endif
 
 // Division sites that use the FP64 pipe's IEEE division instead of the integer-pipe one, one bit
 // per site: 0 EOS gamma p / rho, 1 Godunov, 2 GAD ratios, 3 GAD dt / Dm, 4 Lagrange dm / W,
@@ -209,6 +214,17 @@ template <int G, int MASK = ARMON_SOFT_MUL> __device__ __forceinline__ double qm
     return (ARMON_SOFT_FP64 && (((ARMON_SOFT_MUL | MASK) >> G) & 1)) ? sfp::mul(a, b) : a * b;
 }
 template <int G, int MASK = ARMON_SOFT_MUL> __device__ __forceinline__ float qmul(float a, float b) { return a * b; }
+// a + b and a - b (== a + (-b) for non-NaN b), on the integer pipes for the stages in MASK
+template <int G, int MASK> __device__ __forceinline__ double qadd(double a, double b)
+{
+    return (ARMON_SOFT_FP64 && ((MASK >> G) & 1)) ? sfp::add(a, b) : a + b;
+}
+template <int G, int MASK> __device__ __forceinline__ float qadd(float a, float b) { return a + b; }
+template <int G, int MASK> __device__ __forceinline__ double qsub(double a, double b)
+{
+    return (ARMON_SOFT_FP64 && ((MASK >> G) & 1)) ? sfp::add(a, sfp::neg_if(b, true)) : a - b;
+}
+template <int G, int MASK> __device__ __forceinline__ float qsub(float a, float b) { return a - b; }
 // Kokkos::min / Kokkos::max: (b < a) ? b : a and (a < b) ? b : a
 template <class T> __device__ __forceinline__ T qmin(T a, T b) { return qlt(b, a) ? b : a; }
 template <class T> __device__ __forceinline__ T qmax(T a, T b) { return qlt(a, b) ? b : a; }
@@ -281,45 +297,46 @@ __device__ __forceinline__ void eos(CellIn<T>& c, T gamma, T gamma_m1)
     c.c = ((ARMON_HW_DIV >> 9) & 1) ? sqrt(q) : qsqrt(q);
 }
 
-template <class T>
+template <class T, int ADDS = 0>
 __device__ __forceinline__ God<T> godunov(const CellIn<T>& L, const CellIn<T>& R)
 {
     // src/kernels/acoustic.cpp:10-19 (face between L = i-s and R = i); rc_l * L.ua == L.rcu
     God<T> g;
-    g.rcs = L.rc + R.rc;
+    g.rcs = qadd<2, ADDS>(L.rc, R.rc);
     const auto inv = qrecip_at<1>(g.rcs);
-    g.us = qdiv_at<1>(L.rcu + R.rcu + (L.p - R.p), inv);
-    g.ps = qdiv_at<1>(qmul<2>(R.rc, L.p) + qmul<2>(L.rc, R.p) + qmul<2>(qmul<2>(L.rc, R.rc), L.ua - R.ua), inv);
+    g.us = qdiv_at<1>(qadd<2, ADDS>(qadd<2, ADDS>(L.rcu, R.rcu), qsub<2, ADDS>(L.p, R.p)), inv);
+    g.ps = qdiv_at<1>(qadd<2, ADDS>(qadd<2, ADDS>(qmul<2>(R.rc, L.p), qmul<2>(L.rc, R.p)),
+                                    qmul<2>(qmul<2>(L.rc, R.rc), qsub<2, ADDS>(L.ua, R.ua))), inv);
     return g;
 }
 
-template <class T>
+template <class T, int ADDS = 0>
 __device__ __forceinline__ GadDiff<T> gad_diff(const God<T>& G, const CellIn<T>& Cl, const CellIn<T>& Cr)
 {
     GadDiff<T> d;
-    d.au = G.us - Cl.ua;
-    d.bu = Cr.ua - G.us;
-    d.ap = G.ps - Cl.p;
-    d.bp = Cr.p - G.ps;
+    d.au = qsub<3, ADDS>(G.us, Cl.ua);
+    d.bu = qsub<3, ADDS>(Cr.ua, G.us);
+    d.ap = qsub<3, ADDS>(G.ps, Cl.p);
+    d.bp = qsub<3, ADDS>(Cr.p, G.ps);
     return d;
 }
 
-template <class T, int MULS = ARMON_SOFT_MUL>
+template <class T, int MULS = ARMON_SOFT_MUL, int ADDS = 0>
 __device__ __forceinline__ Flux<T> gad(const God<T>& Gc, const GadDiff<T>& Dm1, const GadDiff<T>& D0,
                                        const GadDiff<T>& Dp1, T dm_l, T dm_r, int L, T dt)
 {
     // src/kernels/acoustic.cpp:40-88 for face i (between cells i-s and i), with the differences
     // of faces i-s (Dm1), i (D0), i+s (Dp1):  Gp.us - Cr.ua == Dp1.au, Gc.us - Cl.ua == D0.au,
     // Cl.ua - Gm.us == Dm1.bu, Cr.ua - Gc.us == D0.bu (the same for p).
-    const T r_um = limited_ratio(L, Dp1.au, D0.au + T(1e-6));
-    const T r_pm = limited_ratio(L, Dp1.ap, D0.ap + T(1e-6));
-    const T r_up = limited_ratio(L, Dm1.bu, D0.bu + T(1e-6));
-    const T r_pp = limited_ratio(L, Dm1.bp, D0.bp + T(1e-6));
-    T Dm = qhalf(dm_l + dm_r);                           // (dm_l + dm_r) / 2
-    T theta = qhalf(1 - qmul<3, MULS>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm)));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
+    const T r_um = limited_ratio(L, Dp1.au, qadd<3, ADDS>(D0.au, T(1e-6)));
+    const T r_pm = limited_ratio(L, Dp1.ap, qadd<3, ADDS>(D0.ap, T(1e-6)));
+    const T r_up = limited_ratio(L, Dm1.bu, qadd<3, ADDS>(D0.bu, T(1e-6)));
+    const T r_pp = limited_ratio(L, Dm1.bp, qadd<3, ADDS>(D0.bp, T(1e-6)));
+    T Dm = qhalf(qadd<3, ADDS>(dm_l, dm_r));              // (dm_l + dm_r) / 2
+    T theta = qhalf(qsub<3, ADDS>(T(1), qmul<3, MULS>(qhalf(Gc.rcs), qdiv_at<3>(dt, Dm))));   // 0.5 (1 - (rc_l + rc_r) / 2 dt / Dm)
     Flux<T> f;
-    f.us = Gc.us + qmul<3, MULS>(theta, qmul<3, MULS>(r_up, D0.bu) - qmul<3, MULS>(r_um, D0.au));
-    f.ps = Gc.ps + qmul<3, MULS>(theta, qmul<3, MULS>(r_pp, D0.bp) - qmul<3, MULS>(r_pm, D0.ap));
+    f.us = qadd<3, ADDS>(Gc.us, qmul<3, MULS>(theta, qsub<3, ADDS>(qmul<3, MULS>(r_up, D0.bu), qmul<3, MULS>(r_um, D0.au))));
+    f.ps = qadd<3, ADDS>(Gc.ps, qmul<3, MULS>(theta, qsub<3, ADDS>(qmul<3, MULS>(r_pp, D0.bp), qmul<3, MULS>(r_pm, D0.ap))));
     return f;
 }
 

@@ -83,7 +83,7 @@ __device__ __forceinline__ bool load_position(const AxisGeom<T>& g, int n, int s
 }
 
 // ---- the face half: EOS of the cells, Godunov state of each face, GAD (or Godunov) flux ----
-template <class T, int SCHEME, int PROJ, bool LAST, int MULS = ARMON_SOFT_MUL>
+template <class T, int SCHEME, int PROJ, bool LAST, int MULS = ARMON_SOFT_MUL, int ADDS = 0>
 __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk, const int pass)
 {
     constexpr bool kGAD = SCHEME == 1;
@@ -147,13 +147,13 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
             }
             if (t >= t0 + 1) {
                 G1 = G2;
-                G2 = godunov(C1, C2);
-                if (kGAD) { D0 = D1; D1 = D2; D2 = gad_diff(G2, C1, C2); }
+                G2 = godunov<T, ADDS>(C1, C2);
+                if (kGAD) { D0 = D1; D1 = D2; D2 = gad_diff<T, ADDS>(G2, C1, C2); }
             }
             if (kGAD ? (t >= t0 + 3) : (t >= t0 + 1)) {
                 Flux<T> f;
                 if (kGAD) {
-                    f = gad<T, MULS>(G1, D0, D1, D2, C0.dm, C1.dm, A.limiter, dt);
+                    f = gad<T, MULS, ADDS>(G1, D0, D1, D2, C0.dm, C1.dm, A.limiter, dt);
                 } else {
                     f.us = G2.us; f.ps = G2.ps;
                 }
@@ -324,7 +324,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
 template <class T, int SCHEME, int PROJ, bool LAST>
 __global__ void __launch_bounds__(128, sweep_faces_min_blocks<T>()) sweep_faces_kernel(const SweepArgs<T> A)
 {
-    sweep_faces<T, SCHEME, PROJ, LAST, ARMON_FACES_SOFT_MUL>(A, blockIdx.x, A.pass);
+    sweep_faces<T, SCHEME, PROJ, LAST, ARMON_FACES_SOFT_MUL, ARMON_FACES_SOFT_ADD>(A, blockIdx.x, A.pass);
 }
 
 template <class T, int SCHEME, int PROJ, bool LAST>

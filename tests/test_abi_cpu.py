@@ -124,3 +124,16 @@ def test_split_pass_positions_stay_inside_the_required_ghosts(gad, second_order)
             lo, hi = min(lo, t0 - 1), max(hi, t1 - 1)                # cell t - 1 of each iteration
         assert written == set(range(-r, n + r + 1)) and -2 <= -r and n + r <= n + 2   # n + 5 faces a line
         assert -reach <= lo and hi <= n + reach - 1, (n, seg, lo, hi, reach)
+
+
+def test_soft_addition_matches_ieee_addition_on_the_host():
+    # csrc/softfp.cuh add_bits (the integer-pipe FP64 addition, compiled for the host here) against
+    # the host's IEEE addition on generated operands: every bit class, cancellations, ties, every
+    # exponent, overflow and underflow ranges, zeros
+    L = A.lib()
+    L.armon_selftest_add_host.argtypes = [C.c_uint64, C.c_int64, C.POINTER(C.c_uint64)]
+    for seed in (0x9E3779B97F4A7C15, 0x0F1E2D3C4B5A6978):
+        out = (C.c_uint64 * 4)()
+        assert L.armon_selftest_add_host(seed, 10_000_000, out) == 0
+        assert out[0] == 0, f"{out[0]} mismatches, first a=0x{out[2]:016x} b=0x{out[3]:016x}"
+        assert out[1] > 9_900_000

@@ -260,7 +260,7 @@ struct Tiling {
     int block;
     bool operator==(const Tiling& o) const { return seg[0] == o.seg[0] && seg[1] == o.seg[1] && block == o.block; }
 };
-std::map<std::array<int, 7>, Tiling> g_tilings;
+std::map<std::array<int, 9>, Tiling> g_tilings;
 std::mutex g_tilings_mu;
 
 int launch_pass0(armon_solver* s)
@@ -353,8 +353,8 @@ int tune_tiling(armon_solver* s)
     s->tuned = true;
     const armon_params& p = s->p;
     if ((int64_t)p.nx * p.ny < (1 << 20)) return ARMON_OK;
-    const std::array<int, 7> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting,
-                                 s->o.block_lines};
+    const std::array<int, 9> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting,
+                                 s->o.block_lines, s->split ? 1 : 0, s->ordered ? 1 : 0};
     {
         std::lock_guard<std::mutex> lk(g_tilings_mu);
         auto it = g_tilings.find(key);

@@ -68,7 +68,7 @@ class SodInterface(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("memory_budget", C.c_int64), ("cycles_per_step", C.c_int32), ("block_lines", C.c_int32),
-                ("max_inflight_cells", C.c_int64), ("reserved", C.c_int32 * 2)]
+                ("max_inflight_cells", C.c_int64), ("waves", C.c_int32), ("reserved", C.c_int32)]
 
 
 class RequestInfo(C.Structure):
@@ -465,13 +465,14 @@ class Server:
     """The request loop over batches (armon_server_* of include/armon_gb300.h)."""
 
     def __init__(self, memory_budget: int = 150_000_000_000, cycles_per_step: int = 8, block_lines: int = 128,
-                 max_inflight_cells: int | None = None):
+                 max_inflight_cells: int | None = None, waves: int = 0):
         L = lib()
         o = ServerOpts()
         L.armon_server_opts_default(C.byref(o))
         o.memory_budget, o.cycles_per_step, o.block_lines = memory_budget, cycles_per_step, block_lines
         if max_inflight_cells is not None:
             o.max_inflight_cells = max_inflight_cells
+        o.waves = waves
         h = C.c_void_p()
         check(L.armon_server_create(C.byref(o), C.byref(h)))
         self._h = h

@@ -77,6 +77,7 @@ int batch_for(armon_server* s, const armon_params& p, int32_t precision, armon_b
     bo.precision = precision;
     bo.cycles_per_graph = s->o.cycles_per_step;
     bo.block_lines = s->o.block_lines;
+    bo.waves = s->o.waves;
     armon_batch* b = nullptr;
     int rc = armon_batch_create(&bo, nullptr, &b);   // its own stream
     if (rc != ARMON_OK) return rc;

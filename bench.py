@@ -481,7 +481,7 @@ def run_serve(args) -> None:
     with A.Server(cycles_per_step=args.serve_cycles) as srv:
         S.replay(srv, W.serving_trace(n=4, rate=1000.0, seed=1, side_range=(128, 128)))
     with A.Server(memory_budget=150_000_000_000, cycles_per_step=args.serve_cycles,
-                  max_inflight_cells=args.max_inflight) as srv:
+                  max_inflight_cells=args.max_inflight, waves=args.serve_waves) as srv:
         sampler = ClockSampler()
         sampler.start()
         served, wall = S.replay(srv, trace)
@@ -558,6 +558,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="--workload serve: requests of the trace")
     ap.add_argument("--rate", type=float, default=50.0, help="--workload serve: arrivals per second")
     ap.add_argument("--serve-cycles", type=int, default=8, help="--workload serve: cycles per round")
+    ap.add_argument("--serve-waves", type=int, default=0,
+                    help="--workload serve: block waves the batches' schedules aim for (0 = autotuned)")
     ap.add_argument("--plain-sample", type=int, default=100, help="--workload serve: requests timed on the plain path")
     ap.add_argument("--accuracy-sample", type=int, default=5, help="--workload serve: FP32 requests checked against FP64")
     ap.add_argument("--max-inflight", type=int, default=None,

@@ -266,7 +266,8 @@ typedef struct armon_server_opts {
     int64_t max_inflight_cells;/* real cells running at once in one batch (0 = no limit): beyond
                                   what saturates the GPU, more solves at once only share it, and
                                   every one of them finishes later */
-    int32_t reserved[2];
+    int32_t waves;             /* as armon_batch_opts.waves for every batch (0 = autotuned) */
+    int32_t reserved;
 } armon_server_opts;
 
 enum { ARMON_REQ_QUEUED = 0, ARMON_REQ_RUNNING = 1, ARMON_REQ_DONE = 2, ARMON_REQ_FAILED = 3 };

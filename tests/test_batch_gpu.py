@@ -180,3 +180,20 @@ def test_split_and_fused_batch_passes_agree_bitwise():
         assert ca == cb and ta == tb
         for k in FIELDS:
             assert np.array_equal(fa[k].view(np.int64), fb[k].view(np.int64)), k
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_longest_first_batch_dispatch_keeps_results(precision):
+    # the blocks of all domains launched by the previous cycle's costs or in index order
+    specs = small_domains(9, seed=31, sides=(24, 40, 64, 96, 130))
+    out = []
+    for order in (0, -1):
+        with A.Batch(precision=precision, cycles_per_graph=4, unit_order=order) as b:
+            ids = [b.add(s.params(), s.initial_state()) for s in specs]
+            assert b.run() == 0
+            out.append([(b.state(i)[0].cycle, b.state(i)[0].time, {k: b.download(i, k) for k in FIELDS})
+                        for i in ids])
+    for (ca, ta, fa), (cb, tb, fb) in zip(*out):
+        assert ca == cb and ta == tb
+        for k in FIELDS:
+            assert np.array_equal(fa[k].view(np.int64), fb[k].view(np.int64)), k

@@ -34,6 +34,10 @@
 // State.  Each pass reads one buffer set and writes the other (in-place updates would race across
 // segment halos); the current set is (cycles_done * passes_per_cycle) % 2.  The pass also writes
 // p, c, g of its input (what update_EOS leaves in memory) for the real cells when asked.
+//
+// This file holds the stage functions, the fused kernels (the FP32 pass, and the FP64 pass on
+// request) and the batch kernel; sweep_split.cuh runs the same stages as two launches per pass (the
+// FP64 default), and order.cuh orders each launch's units longest first.
 #pragma once
 
 #include "device_common.cuh"

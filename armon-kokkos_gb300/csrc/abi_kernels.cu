@@ -67,6 +67,10 @@ void launch_range(const Range* r, F f)
     check_cuda(cudaGetLastError(), "kernel launch");
 }
 
+// The entry point being run, for the label check's message (the checks run inside the lambda that
+// guarded() calls, where __func__ would name the lambda).
+thread_local const char* g_kernel = "";
+
 // CHECK_VIEW_LABELS (src/kernels/utils.h:74-96): a labelled view must end with the parameter name.
 void check_label(const view* v, const char* name, const char* func)
 {
@@ -76,12 +80,13 @@ void check_label(const view* v, const char* name, const char* func)
     throw std::invalid_argument(std::string("Wrong view order in ") + func + ": expected " + name + ", got: " +
                                 v->label + "\n");
 }
-#define CHECK_LABEL(v) check_label(v, #v, __func__)
+#define CHECK_LABEL(v) check_label(v, #v, g_kernel)
 
 // KERNEL_TRY / KERNEL_CATCH -> raise_exception (src/kernels/utils.h:103-114, utils.cpp:49-54)
 template <class Body>
 void guarded(const char* kernel, Body body)
 {
+    g_kernel = kernel;
     try {
         body();
     } catch (const std::invalid_argument& e) {
@@ -93,18 +98,30 @@ void guarded(const char* kernel, Body body)
     }
 }
 
-// Device scratch for the two reductions: one pair of doubles per block, kept between calls.
+// Device scratch for the two reductions: one pair of doubles per block, kept between calls, one
+// buffer per device (a buffer is only valid on the device that allocated it).  Host threads that
+// call the reductions at the same time on one device share the buffer and race on it, as they
+// share the library's stream; the lock only protects the allocation itself.
 double* scratch(size_t doubles)
 {
-    static double* buf = nullptr;
-    static size_t cap = 0;
-    if (doubles > cap) {
-        if (buf) cudaFree(buf);
-        buf = nullptr;
-        check_cuda(cudaMalloc(&buf, doubles * sizeof(double)), "cudaMalloc");
-        cap = doubles;
+    static std::mutex mu;
+    static double* buf[64] = {};
+    static size_t cap[64] = {};
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range for the scratch table");
+    std::lock_guard<std::mutex> lk(mu);
+    if (doubles > cap[dev]) {
+        if (buf[dev]) {
+            check_cuda(cudaStreamSynchronize(g_stream), "cudaStreamSynchronize");
+            cudaFree(buf[dev]);
+        }
+        buf[dev] = nullptr;
+        cap[dev] = 0;
+        check_cuda(cudaMalloc(&buf[dev], doubles * sizeof(double)), "cudaMalloc");
+        cap[dev] = doubles;
     }
-    return buf;
+    return buf[dev];
 }
 
 __device__ __forceinline__ void godunov(double rho_i, double rho_im, double c_i, double c_im, double u_i, double u_im,
@@ -305,7 +322,7 @@ void acoustic_GAD(const Range* range, const InnerRange2D* inner_range, Idx s, fl
         double *ust = ustar->data, *pst = pstar->data;
         const double *rh = rho->data, *uu = u->data, *p = pmat->data, *c = cmat->data;
         launch_range(range, [=] __device__(int64_t k) {
-            // src/kernels/acoustic.cpp:109-148
+            // src/kernels/acoustic.cpp:40-88
             int64_t i = scale2d(ir, (uint64_t)k);
             double ustar_im, pstar_im, ustar_i, pstar_i, ustar_ip, pstar_ip;
             godunov(rh[i - s], rh[i - 2 * s], c[i - s], c[i - 2 * s], uu[i - s], uu[i - 2 * s], p[i - s], p[i - 2 * s],

@@ -151,7 +151,10 @@ flt_t dt_CFL(const Range* range, const InnerRange1D* inner_range, flt_t dx, flt_
  *  - Limit: ranges of at most 134,217,728 indices (32768 tiles of 4096); a longer range goes to
  *    raise_exception_handler with an out_of_range message.
  *  - The first call on each device resolves the array's device address (cudaGetSymbolAddress with
- *    that device current); make that first call before any stream capture.
+ *    that device current); make that first call before any stream capture.  With CUDA's lazy
+ *    module loading (the default), that call may also be what loads the library's device module
+ *    and reserves the array, so make it, or any earlier call into the library, before the host
+ *    hands the device's free memory to its own pool.
  *  - Every call shares the one array (it keeps the last call's partials; each call overwrites all
  *    it reads), so calls that overlap on the GPU race: issue them on one stream.
  *  - Every GPU that loads the library holds the array until the process exits. */

@@ -8,6 +8,18 @@
  *   keys: test scheme projection limiter splitting nghost nx ny stencil cfl dt cst_dt
  *         dt_on_even_cycles max_cycles max_time size_x size_y origin_x origin_y test_option
  *         stage_dump_cycles (>0: also dump after every stage of the first N cycles)
+ *         border_dump (1: the border-array records below instead of a time loop)
+ *
+ * Border records (border_dump=1): the seven fields read_border_array packs get exact integer
+ * values f(k, i) = ((37 i + 1013 k) mod 65521) - 30000 (k = rho, umat, vmat, pmat, cmat, gmat,
+ * Emat; i the linear cell index).  For each side (left, right, bottom, top: the nghost real
+ * columns or rows next to that edge) read_border_array (src/kernels/halo_exchange.cpp:39-64)
+ * packs them; the record is char tag[32]; int64 range_start, range_end, main_range_start,
+ * main_range_step, row_range_start, row_range_length, side_length, nghost, n; float64 values[n].
+ * Then write_border_array (:67-92) unpacks 2 v + 1 of every side's values, in side order, and one
+ * "final" state record follows.  Left and right iterate rows of nghost cells (side_length = ny),
+ * bottom and top nghost rows of nx cells (side_length = nx), so their packing order is the
+ * reference's index arithmetic applied to that range.
  *
  * File layout (little endian): repeated records of
  *   char tag[32]; int32 cycle, axis, nb_cells, status; float64 current_dt, next_dt, time, cycle_dt;
@@ -15,7 +27,16 @@
  *                                   work_array_1..4 domain_mask)
  *
  * test_option: the reference's Sod_circ ignores it; a Sod_circ radius other than 0.3 is
- * therefore not available from the reference and is only exercised through the oracle.
+ * therefore not available from the reference's init_test.  radius2=r2 (Sod_circ only) re-labels
+ * the cells of init_test's high region that lie outside the squared radius r2 with the low state,
+ * by the same cell-centre test (src/kernels/test_cases.h:72-76, init_test.cpp:62-90), so that the
+ * reference starts from the same state as a solver given that radius.
+ *
+ * Timing mode (the CPU baseline of the benchmark): out = "-" and bench_cycles=K runs the
+ * reference's own time_loop (src/armon_2D.cpp:327-386) twice, bench_warmup=W cycles and then K
+ * cycles, on the host cores (OpenMP through the shim), and prints the reference's own timing lines
+ * of the second run plus one line "bench cycles=.. seconds=.. grind_us=.. threads=..".  The timing
+ * build (oracle/Makefile ref-fast) uses the reference's Release flags.
  */
 #include "armon_2D.h"
 #include "parameters.h"
@@ -25,6 +46,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
+#include <omp.h>
 
 static FILE* g_out = nullptr;
 
@@ -53,7 +76,8 @@ int main(int argc, char** argv)
 {
     if (argc < 2) { std::fprintf(stderr, "usage: ref_driver out.bin key=value...\n"); return 2; }
     Params p;
-    int stage_dump_cycles = 0;
+    int stage_dump_cycles = 0, bench_cycles = 0, bench_warmup = 0, border_dump = 0;
+    double radius2 = 0;
     static const char* tests[] = {"Sod", "Sod_y", "Sod_circ", "Bizarrium", "Sedov"};
     static const char* schemes[] = {"Godunov", "GAD"};
     static const char* projs[] = {"none", "euler", "euler_2nd"};
@@ -85,18 +109,93 @@ int main(int argc, char** argv)
         else if (k == "origin_x") p.domain_origin[0] = std::stod(v);
         else if (k == "origin_y") p.domain_origin[1] = std::stod(v);
         else if (k == "stage_dump_cycles") stage_dump_cycles = std::stoi(v);
+        else if (k == "bench_cycles") bench_cycles = std::stoi(v);
+        else if (k == "bench_warmup") bench_warmup = std::stoi(v);
+        else if (k == "radius2") radius2 = std::stod(v);
+        else if (k == "border_dump") border_dump = std::stoi(v);
         else ok = false;
         if (!ok) { std::fprintf(stderr, "bad arg %s\n", argv[a]); return 2; }
     }
-    p.verbose = 5;
+    p.verbose = bench_cycles > 0 ? 2 : 5;
     p.init();
     if (!p.check()) { std::fprintf(stderr, "invalid parameters\n"); return 3; }
 
-    g_out = std::fopen(argv[1], "wb");
-    if (!g_out) return 4;
+    const bool to_file = std::strcmp(argv[1], "-") != 0;
+    if (to_file) {
+        g_out = std::fopen(argv[1], "wb");
+        if (!g_out) return 4;
+    }
 
     Data d(p.nb_cells, "Armon_");
     init_test(p, d);
+    if (radius2 > 0 && p.test == Test::Sod_circ) {
+        /* the low state, as init_test wrote it in the corner real cell (outside any radius <= 0.5) */
+        const Idx c0 = p.index_start;
+        const flt_t low_rho = d.rho[c0], low_E = d.Emat[c0], low_u = d.umat[c0], low_v = d.vmat[c0];
+        const flt_t sx = p.domain_size[0], sy = p.domain_size[1];
+        for (Idx i = 0; i < p.nb_cells; i++) {
+            flt_t x_mid = d.x[i] + sx / flt_t(2 * p.nx);
+            flt_t y_mid = d.y[i] + sy / flt_t(2 * p.ny);
+            flt_t r2 = (x_mid - flt_t(0.5)) * (x_mid - flt_t(0.5)) + (y_mid - flt_t(0.5)) * (y_mid - flt_t(0.5));
+            if (!(r2 <= flt_t(radius2))) {
+                d.rho[i] = low_rho; d.Emat[i] = low_E; d.umat[i] = low_u; d.vmat[i] = low_v;
+            }
+        }
+    }
+    if (bench_cycles > 0) {
+        HostData hd{0};
+        if (bench_warmup > 0) {
+            p.max_cycles = bench_warmup;
+            p.verbose = 5;
+            time_loop(p, d, hd);
+        }
+        p.max_cycles = bench_cycles;
+        p.verbose = 2;
+        auto [grind, dt, cycles] = time_loop(p, d, hd);
+        std::fprintf(stdout, "bench cycles=%d seconds=%.9g grind_us=%.9g threads=%d\n", cycles,
+                     grind * 1e-6 * double(cycles) * p.nx * p.ny, grind, omp_get_max_threads());
+        return 0;
+    }
+    if (!to_file) { std::fprintf(stderr, "an output file is needed outside the timing mode\n"); return 2; }
+    if (border_dump) {
+        view* fields[7] = {&d.rho, &d.umat, &d.vmat, &d.pmat, &d.cmat, &d.gmat, &d.Emat};
+        for (int k = 0; k < 7; k++)
+            for (Idx i = 0; i < p.nb_cells; i++)
+                (*fields[k])[i] = flt_t((37 * (int64_t)i + 1013 * k) % 65521) - 30000.0;
+        const Idx g = p.nb_ghosts, R = p.row_length, c0 = p.index_start;
+        struct Side { const char* tag; InnerRange2D ir; Idx side_length; };
+        const Side sides[4] = {
+            {"border_left", {c0, R, 0, (UIdx)g}, p.ny},
+            {"border_right", {c0 + p.nx - g, R, 0, (UIdx)g}, p.ny},
+            {"border_bottom", {c0, R, 0, (UIdx)p.nx}, p.nx},
+            {"border_top", {c0 + (p.ny - g) * R, R, 0, (UIdx)p.nx}, p.nx},
+        };
+        std::vector<view> packed;
+        for (const Side& sd : sides) {
+            const Idx n = 7 * g * sd.side_length;
+            Range r{0, g * sd.side_length};
+            view va("value_array", n);
+            read_border_array(r, sd.ir, sd.side_length, g, d.rho, d.umat, d.vmat, d.pmat, d.cmat, d.gmat, d.Emat, va);
+            char t[32] = {0};
+            std::strncpy(t, sd.tag, 31);
+            std::fwrite(t, 1, 32, g_out);
+            int64_t hdr[9] = {r.start, r.end, sd.ir.main_range_start, sd.ir.main_range_step, sd.ir.row_range_start,
+                              (int64_t)sd.ir.row_range_length, sd.side_length, g, n};
+            std::fwrite(hdr, sizeof(int64_t), 9, g_out);
+            std::fwrite(va.data(), sizeof(double), (size_t)n, g_out);
+            packed.push_back(va);
+        }
+        for (int k = 0; k < 4; k++) {
+            const Side& sd = sides[k];
+            view va("value_array", 7 * g * sd.side_length);
+            for (Idx i = 0; i < 7 * g * sd.side_length; i++) va[i] = 2 * packed[k][i] + 1;
+            Range r{0, g * sd.side_length};
+            write_border_array(r, sd.ir, sd.side_length, g, d.rho, d.umat, d.vmat, d.pmat, d.cmat, d.gmat, d.Emat, va);
+        }
+        dump(p, d, "final", 0);
+        std::fclose(g_out);
+        return 0;
+    }
     {
         /* the test option the reference's init_test used (src/armon_2D.cpp:116-118) */
         flt_t dx = p.domain_size[0] / flt_t(p.nx), dy = p.domain_size[1] / flt_t(p.ny);

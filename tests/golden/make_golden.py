@@ -10,8 +10,9 @@ cases below and writes:
                    (all cells, ghosts included) after every stage of the first two cycles;
   fields_*.npz     the real-cell fields of a few small cases, for readable diffs.
 
-The reference tree is only needed to regenerate the fixtures (python tests/golden/make_golden.py
-with the reference at $ARMON_REF, default /root/reference).  The tests only read the fixtures.
+The reference tree is only needed to regenerate the fixtures: python tests/golden/make_golden.py
+compiles the tree at $ARMON_REF, else the copy that `make -C oracle stage` puts in baseline/_ref.
+The tests only read the fixtures.
 """
 from __future__ import annotations
 
@@ -74,6 +75,11 @@ def ref_cases() -> dict[str, O.Case]:
         "sod_circ_gad_256_cfl06": O.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5,
                                          nx=256, ny=256, cfl=0.6, max_cycles=20, max_time=1e9),
     }
+    # the benchmark's circular Sod at radius 0.2 (configuration 2 shrunk): the reference's init_test
+    # hard-codes radius 0.3, so ref_driver re-labels the cells outside 0.2 (its radius2 option)
+    for name, (nx, ny, cyc) in {"sod_circ_r02_gad_160x96": (160, 96, 12), "sod_circ_r02_gad_512": (512, 512, 30)}.items():
+        cases[name] = O.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=nx, ny=ny,
+                             cfl=0.6, max_cycles=cyc, max_time=1e9, test_option=0.04)
     # tests/armon_2D_tests.cpp:246-275: 400 cycles, max_time 1e4, conservation to 1e-12
     for t in ("Sod", "Sod_y", "Sod_circ", "Sedov"):
         c = dict(ref)
@@ -98,13 +104,53 @@ def field_hashes(p: O.OParams, rec: dict) -> dict[str, str]:
 
 def run_ref(case: O.Case, out: str, extra: list[str] | None = None) -> tuple[list[dict], str]:
     env = dict(os.environ, OMP_NUM_THREADS="1")
+    if case.test == "Sod_circ" and case.test_option > 0:
+        extra = (extra or []) + [f"radius2={case.test_option!r}"]
     r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_driver"), out] + case.driver_args()
                        + (extra or []), check=True, capture_output=True, text=True, env=env)
     return O.read_ref_dump(out), r.stdout
 
 
+BORDER_CASE = O.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=20, ny=12)
+
+
+def read_border_records(path: str) -> tuple[list[dict], dict]:
+    """The border records of ref_driver's border_dump mode, then its final state record."""
+    raw = open(path, "rb").read()
+    off, sides = 0, []
+    while raw[off:off + 32].split(b"\0", 1)[0].decode().startswith("border_"):
+        tag = raw[off:off + 32].split(b"\0", 1)[0].decode()
+        hdr = np.frombuffer(raw, dtype=np.int64, count=9, offset=off + 32)
+        n = int(hdr[8])
+        vals = np.frombuffer(raw, dtype=np.float64, count=n, offset=off + 32 + 72).copy()
+        sides.append({"tag": tag, "range": [int(hdr[0]), int(hdr[1])],
+                      "inner": [int(x) for x in hdr[2:6]], "side_length": int(hdr[6]), "nghost": int(hdr[7]),
+                      "values": vals})
+        off += 32 + 72 + 8 * n
+    tmp = path + ".final"
+    with open(tmp, "wb") as f:
+        f.write(raw[off:])
+    final = O.read_ref_dump(tmp)[0]
+    os.remove(tmp)
+    return sides, final
+
+
+def border_fixture(tmp: str) -> dict:
+    """read_border_array / write_border_array (src/kernels/halo_exchange.cpp:39-92) of the
+    reference on the four borders of a 20x12 domain with 5 ghosts (ref_driver border_dump)."""
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_driver"), tmp] + BORDER_CASE.driver_args()
+                   + ["border_dump=1"], check=True, capture_output=True, text=True)
+    sides, final = read_border_records(tmp)
+    np.savez_compressed(os.path.join(HERE, "borders_20x12.npz"), **{s["tag"]: s["values"] for s in sides})
+    return {"case": BORDER_CASE.__dict__,
+            "sides": [{k: (sha(v) if k == "values" else v) for k, v in s.items()} for s in sides],
+            "final_hashes": {k: sha(final[k]) for k in ("rho", "umat", "vmat", "pmat", "cmat", "gmat", "Emat")}}
+
+
 def main() -> None:
-    ref_dir = os.environ.get("ARMON_REF", "/root/reference")
+    ref_dir = os.environ.get("ARMON_REF", os.path.join(ROOT, "baseline", "_ref"))
+    if not os.path.isdir(os.path.join(ref_dir, "src", "kernels")):
+        raise SystemExit(f"no reference tree at {ref_dir}: set ARMON_REF or run make -C oracle stage")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref_dir}", "-j8"],
                    check=True, capture_output=True)
     gold: dict = {"cases": {}, "stages": {}}
@@ -142,6 +188,7 @@ def main() -> None:
          "current_cycle_dt": r["current_cycle_dt"].hex(), "next_cycle_dt": r["next_cycle_dt"].hex(),
          "cycle_dt": r["cycle_dt"].hex(),
          "hashes": {k: sha(r[k]) for k in O.ARRAY_NAMES}} for r in recs]}
+    gold["borders"] = border_fixture(tmp)
     os.remove(tmp)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(gold, f, indent=1, sort_keys=True)

@@ -124,6 +124,10 @@ def lib(fast: bool = False) -> C.CDLL:
     L.o_scale_index_2d.argtypes = [OInner2D, C.c_uint64]
     L.o_scale_index_2d.restype = C.c_int64
     L.o_boundary_factors.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    DP = C.POINTER(C.c_double)
+    for fn in ("o_read_border_array", "o_write_border_array"):
+        getattr(L, fn).argtypes = [ORange, OInner2D, C.c_int64, C.c_int64] + [DP] * 8
+        getattr(L, fn).restype = None
     _LIBS[name] = L
     return L
 

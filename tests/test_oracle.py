@@ -175,3 +175,39 @@ def test_ghost_requirement_check():
     assert p.stencil_width == 4 and not L.o_params_check(C.byref(p))
     p = O.make_params(O.Case(test="Sod", scheme="Godunov", projection="euler", nghost=3, nx=10, ny=10))
     assert p.stencil_width == 1 and L.o_params_check(C.byref(p))
+
+
+BORDERS = GOLDEN["borders"]
+BORDER_FIELDS = ("rho", "umat", "vmat", "pmat", "cmat", "gmat", "Emat")
+
+
+def border_inputs(p):
+    """The field values the reference's border records were made from: exact integers
+    ((37 i + 1013 k) mod 65521) - 30000 for field k and linear cell index i."""
+    i = np.arange(p.nb_cells, dtype=np.int64)
+    return {name: ((37 * i + 1013 * k) % 65521 - 30000).astype(np.float64) for k, name in enumerate(BORDER_FIELDS)}
+
+
+def test_border_arrays_match_reference():
+    """read_border_array / write_border_array (src/kernels/halo_exchange.cpp:39-92) of the oracle
+    against the reference's own output on the four borders (tests/golden/borders_20x12.npz)."""
+    L = O.lib()
+    p = O.make_params(O.Case(**BORDERS["case"]))
+    f = border_inputs(p)
+    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    packed = []
+    saved = np.load(os.path.join(os.path.dirname(__file__), "golden", "borders_20x12.npz"))
+    for side in BORDERS["sides"]:
+        r = O.ORange(*side["range"])
+        ir = O.OInner2D(*side["inner"])
+        va = np.full(7 * side["nghost"] * side["side_length"], np.nan)
+        L.o_read_border_array(r, ir, side["side_length"], side["nghost"], *[ptr(f[k]) for k in BORDER_FIELDS], ptr(va))
+        assert sha(va) == side["values"], side["tag"]
+        assert np.array_equal(va, saved[side["tag"]]), side["tag"]
+        packed.append(va)
+    for side, va in zip(BORDERS["sides"], packed):
+        va2 = 2 * va + 1
+        L.o_write_border_array(O.ORange(*side["range"]), O.OInner2D(*side["inner"]), side["side_length"],
+                               side["nghost"], *[ptr(f[k]) for k in BORDER_FIELDS], ptr(va2))
+    for k in BORDER_FIELDS:
+        assert sha(f[k]) == BORDERS["final_hashes"][k], k

@@ -272,41 +272,38 @@ def test_bizarrium_stages_close_to_reference():
         assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max(), k
 
 
-def test_border_arrays_roundtrip():
-    """read_border_array / write_border_array (src/kernels/halo_exchange.cpp:39-92) against the oracle."""
-    p = O.make_params(O.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=20, ny=12))
+def test_border_arrays_match_reference():
+    """read_border_array / write_border_array (src/kernels/halo_exchange.cpp:39-92) through the C ABI
+    against the reference's own output on the four borders (golden "borders": left, right, bottom,
+    top of a 20x12 domain with 5 ghosts), then the unpack of 2 v + 1 of every side."""
+    B = GOLDEN["borders"]
+    p = O.make_params(O.Case(**B["case"]))
     n = p.nb_cells
-    rng = np.random.default_rng(3)
-    host = {k: rng.standard_normal(n) for k in O.ARRAY_NAMES}
+    fields = ("rho", "umat", "vmat", "pmat", "cmat", "gmat", "Emat")
+    i = np.arange(n, dtype=np.int64)
     d = DeviceData(n)
-    for k in O.ARRAY_NAMES:
-        d.t[k].copy_(torch.from_numpy(host[k]))
-    nghost, side = 5, p.ny
-    # the left border: nghost columns of the real rows
-    dom = O.ODomain(p.index_start, p.row_length, p.index_start + (p.ny - 1) * p.row_length, 0, 1, nghost - 1)
-    rg, ir = r2(O.lib(), dom)
-    va = torch.zeros(7 * nghost * side, dtype=torch.float64, device="cuda")
-    vv = A.View(va.data_ptr(), va.numel(), b"value_array")
+    for k, name in enumerate(fields):
+        d.t[name].copy_(torch.from_numpy(((37 * i + 1013 * k) % 65521 - 30000).astype(np.float64)))
     K = A.lib()
-    K.read_border_array.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 8
-    K.read_border_array(C.byref(rg), C.byref(ir), side, nghost, d["rho"], d["umat"], d["vmat"], d["pmat"],
-                        d["cmat"], d["gmat"], d["Emat"], C.byref(vv))
-    ref = np.zeros(7 * nghost * side)
-    ors, oir = O.ORange(rg.start, rg.end), O.OInner2D(ir.main_range_start, ir.main_range_step, ir.row_range_start,
-                                                      ir.row_range_length)
-    ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    O.lib().o_read_border_array(ors, oir, side, nghost, ptr(host["rho"]), ptr(host["umat"]), ptr(host["vmat"]),
-                                ptr(host["pmat"]), ptr(host["cmat"]), ptr(host["gmat"]), ptr(host["Emat"]), ptr(ref))
-    torch.cuda.synchronize()
-    assert np.array_equal(va.cpu().numpy(), ref)
-    # write it back, shifted by 3 rows, on both sides
-    va2 = va * 2.0
-    vv2 = A.View(va2.data_ptr(), va2.numel(), b"value_array")
-    K.write_border_array.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 8
-    K.write_border_array(C.byref(rg), C.byref(ir), side, nghost, d["rho"], d["umat"], d["vmat"], d["pmat"],
-                         d["cmat"], d["gmat"], d["Emat"], C.byref(vv2))
-    ref2 = ref * 2.0
-    O.lib().o_write_border_array(ors, oir, side, nghost, ptr(host["rho"]), ptr(host["umat"]), ptr(host["vmat"]),
-                                 ptr(host["pmat"]), ptr(host["cmat"]), ptr(host["gmat"]), ptr(host["Emat"]), ptr(ref2))
-    for k in ("rho", "umat", "vmat", "pmat", "cmat", "gmat", "Emat"):
-        assert np.array_equal(d.host(k), host[k]), k
+    for fn in ("read_border_array", "write_border_array"):
+        getattr(K, fn).argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 8
+    saved = np.load(os.path.join(os.path.dirname(__file__), "golden", "borders_20x12.npz"))
+    packed = []
+    for side in B["sides"]:
+        rg, ir = A.Range(*side["range"]), A.InnerRange2D(*side["inner"])
+        va = torch.full((7 * side["nghost"] * side["side_length"],), float("nan"), dtype=torch.float64, device="cuda")
+        vv = A.View(va.data_ptr(), va.numel(), b"value_array")
+        K.read_border_array(C.byref(rg), C.byref(ir), side["side_length"], side["nghost"],
+                            *[d[k] for k in fields], C.byref(vv))
+        torch.cuda.synchronize()
+        got = va.cpu().numpy()
+        assert sha(got) == side["values"] and np.array_equal(got, saved[side["tag"]]), side["tag"]
+        packed.append(va)
+    for side, va in zip(B["sides"], packed):
+        va2 = va * 2.0 + 1.0
+        vv2 = A.View(va2.data_ptr(), va2.numel(), b"value_array")
+        K.write_border_array(C.byref(A.Range(*side["range"])), C.byref(A.InnerRange2D(*side["inner"])),
+                             side["side_length"], side["nghost"], *[d[k] for k in fields], C.byref(vv2))
+        torch.cuda.synchronize()
+    for k in fields:
+        assert sha(d.host(k)) == B["final_hashes"][k], k

@@ -6,6 +6,10 @@ device arrays, on consecutive calls and on ranges of different lengths, and chec
 limit.  The file is collected last so that a stop-at-first-failure run has run everything else.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -87,3 +91,33 @@ def test_no_alloc_dt_rejects_ranges_beyond_its_scratch():
         slot.value = saved
     assert messages and messages[0][0] == "dt_CFL_no_alloc"
     assert "static scratch limit" in messages[0][1] and str(MAX_INDICES) in messages[0][1]
+
+
+def test_no_alloc_dt_leaves_device_memory_untouched():
+    """The property the entry point exists for, in a fresh process where nothing else of the
+    library has allocated a reduction buffer: after one warm-up call (which may load the module and
+    so reserve its fixed array), more calls leave the device's free memory exactly as it was."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = textwrap.dedent(f"""
+        import ctypes as C, sys
+        sys.path[:0] = [{here!r}, {os.path.dirname(here)!r}, {os.path.join(os.path.dirname(here), "armon-kokkos_gb300")!r}]
+        import torch
+        import test_zz_no_alloc as T
+        L = T._lib()
+        p, dev = T._device_state()
+        views = T._views(dev)
+        dx, dy = p.domain_size[0] / p.nx, p.domain_size[1] / p.ny
+        rg, ir = T._ranges(p, p.ny)
+        args = (C.byref(rg), C.byref(ir), dx, dy, *[C.byref(v) for v in views])
+        first = L.dt_CFL_no_alloc(*args)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        vals = [L.dt_CFL_no_alloc(*args) for _ in range(5)]
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+        assert all(v == first for v in vals), (first, vals)
+        assert free1 == free0, (free0, free1)
+        print("free bytes unchanged:", free0)
+    """)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -50,13 +50,13 @@ class Params(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("seg_len", C.c_int32),
                 ("block_lines", C.c_int32), ("materialize_eos", C.c_int32), ("unit_order", C.c_int32),
-                ("split_pass", C.c_int32), ("reserved", C.c_int32)]
+                ("split_pass", C.c_int32), ("reuse", C.c_int32)]
 
 
 class BatchOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("cycles_per_graph", C.c_int32), ("block_lines", C.c_int32),
                 ("seg_len", C.c_int32), ("memory_budget", C.c_int64), ("waves", C.c_int32), ("unit_order", C.c_int32),
-                ("split_pass", C.c_int32), ("reserved", C.c_int32)]
+                ("split_pass", C.c_int32), ("reuse", C.c_int32)]
 
 
 class SodInterface(C.Structure):
@@ -234,7 +234,7 @@ class Solver:
 
     def __init__(self, params: Params | Case, precision: int = 64, stream: int | None = None,
                  cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 0,
-                 unit_order: int = 0, split_pass: int = 0):
+                 unit_order: int = 0, split_pass: int = 0, reuse: int = 0):
         L = lib()
         self.params = make_params(params) if isinstance(params, Case) else params
         o = SolverOpts()
@@ -246,6 +246,7 @@ class Solver:
         o.materialize_eos = materialize_eos
         o.unit_order = unit_order
         o.split_pass = split_pass
+        o.reuse = reuse
         self.opts = o
         h = C.c_void_p()
         check(L.armon_solver_create(C.byref(self.params), C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
@@ -354,13 +355,14 @@ class Batch:
 
     def __init__(self, precision: int = 64, stream: int | None = None, cycles_per_graph: int = 8,
                  block_lines: int = 128, seg_len: int = 0, memory_budget: int = 0, waves: int = 0,
-                 unit_order: int = 0, split_pass: int = 0):
+                 unit_order: int = 0, split_pass: int = 0, reuse: int = 0):
         L = lib()
         o = BatchOpts()
         L.armon_batch_opts_default(C.byref(o))
         o.precision, o.cycles_per_graph, o.block_lines = precision, cycles_per_graph, block_lines
         o.seg_len, o.memory_budget, o.waves, o.unit_order = seg_len, memory_budget, waves, unit_order
         o.split_pass = split_pass
+        o.reuse = reuse
         h = C.c_void_p()
         check(L.armon_batch_create(C.byref(o), C.c_void_p(stream or 0), C.byref(h)))
         self._h = h

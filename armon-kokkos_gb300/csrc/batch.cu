@@ -225,7 +225,7 @@ int rebuild_t(armon_batch* b)
         const int fixed = d.seg_len > 0 ? d.seg_len : b->o.seg_len;
         const int forced[2] = {fixed > 0 ? fixed : sched[k][0], fixed > 0 ? fixed : sched[k][1]};
         int nb = make_sweep_args<T>(d.p, b->npass, b->o.block_lines, b->sm_count, forced, buffers<T>(d),
-                                    b->d_states + b->table[k], d.partials, 0, args[k]);
+                                    b->d_states + b->table[k], d.partials, 0, b->o.reuse >= 0 ? 1 : 0, args[k]);
         if (b->split) {
             args[k].faces = static_cast<T*>(d.faces);
             args[k].face_stride = face_values(d.p);

@@ -85,7 +85,7 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
     const int forced[2] = {s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[0],
                            s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[1]};
     s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, forced, b, s->d_state, s->d_partials,
-                                 s->o.materialize_eos, a);
+                                 s->o.materialize_eos, s->o.reuse >= 0 ? 1 : 0, a);
     if (s->split) {
         a.faces = static_cast<T*>(s->d_faces);
         a.face_stride = s->face_stride;

@@ -119,7 +119,8 @@ struct DomainBuffers {
 // larger of its two axes).  forced_seg[axis] > 0 imposes that axis's segment length.
 template <class T>
 int make_sweep_args(const armon_params& p, int npass, int block, int sms, const int forced_seg[2],
-                    const DomainBuffers<T>& b, StepState* state, double* partials, int write_eos, SweepArgs<T>& a)
+                    const DomainBuffers<T>& b, StepState* state, double* partials, int write_eos, int reuse,
+                    SweepArgs<T>& a)
 {
     const int halo = stencil_reach(&p);
     for (int axis = 0; axis < 2; axis++) {
@@ -167,6 +168,7 @@ int make_sweep_args(const armon_params& p, int npass, int block, int sms, const 
     a.npass = npass;
     a.pass = 0;
     a.write_eos = write_eos;
+    a.reuse = reuse;
     a.gamma = T(1.4);   // update_EOS hard-codes gamma = 1.4 (src/armon_2D.cpp:94)
     for (int k = 0; k < 4; k++) { a.buf[0][k] = b.set[0][k]; a.buf[1][k] = b.set[1][k]; }
     a.pmat = b.pmat;

@@ -287,7 +287,7 @@ def run_gpu(args) -> None:
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len,
-                 block_lines=args.block_lines, split_pass=args.split_pass)
+                 block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
     s.init_test()
     s.enqueue_cycles(W)
     torch.cuda.synchronize()
@@ -328,7 +328,7 @@ def run_gpu(args) -> None:
     case_e2e.nx, case_e2e.ny = nx, ny
     case_e2e.max_cycles = K
     se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
-                  seg_len=args.seg_len, block_lines=args.block_lines, split_pass=args.split_pass)
+                  seg_len=args.seg_len, block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
     se.init_test()
     outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
             for k in ("rho", "umat", "vmat", "Emat", "pmat")}
@@ -548,6 +548,9 @@ def main():
     ap.add_argument("--split-pass", type=int, default=0, choices=[-1, 0, 1],
                     help="1: each axis pass as a face launch and a cell launch; -1: one fused launch; "
                          "0: the solver's default (split in FP64)")
+    ap.add_argument("--reuse", type=int, default=0, choices=[-1, 0],
+                    help="0: positions whose input window repeats the previous one reuse its results (exact); "
+                         "-1: every position computed")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--accuracy-cycles", type=int, default=100,

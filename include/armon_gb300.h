@@ -97,7 +97,11 @@ typedef struct armon_solver_opts {
                                  the face buffer, 3 x max((nx+5) ny, (ny+5) nx) values, cannot be
                                  allocated); FP32 passes stay fused.  1: split for either precision;
                                  -1: fused.  Results are the same bits either way. */
-    int32_t reserved;
+    int32_t reuse;            /* 0 (default): along each line, a position whose whole input window
+                                 (the cells, and faces, its results depend on) repeats the previous
+                                 position's bit for bit stores the previous position's results
+                                 instead of recomputing them (fluid at rest); -1: every position is
+                                 computed.  Results are the same bits either way. */
 } armon_solver_opts;
 
 void armon_solver_opts_default(armon_solver_opts* o);
@@ -174,7 +178,7 @@ typedef struct armon_batch_opts {
     int32_t split_pass;       /* as armon_solver_opts.split_pass: 0 (default) split FP64 passes into a
                                  face launch and a cell launch (each domain then holds a face buffer,
                                  counted by armon_batch_domain_bytes); 1: split; -1: fused */
-    int32_t reserved;
+    int32_t reuse;            /* as armon_solver_opts.reuse: 0 (default) on, -1 off */
 } armon_batch_opts;
 
 void armon_batch_opts_default(armon_batch_opts* o);

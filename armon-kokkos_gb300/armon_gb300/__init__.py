@@ -134,6 +134,10 @@ def lib() -> C.CDLL:
     L.armon_solver_kernel_launches.restype = C.c_int64
     L.armon_solver_tiling.argtypes = [S, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.armon_solver_block_lines.argtypes = [S]
+    L.armon_solver_tuning.argtypes = [S]
+    L.armon_solver_split_pass.argtypes = [S]
+    L.armon_tiling_cache_clear.argtypes = []
+    L.armon_tiling_cache_clear.restype = None
     L.armon_solve_host.argtypes = [P, C.POINTER(SolverOpts), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), P]
     B = C.c_void_p
     L.armon_batch_opts_default.argtypes = [C.POINTER(BatchOpts)]
@@ -318,6 +322,19 @@ class Solver:
     def block_lines(self) -> int:
         """Lines (threads) per block of the fused pass."""
         return int(lib().armon_solver_block_lines(self._h))
+
+    def tuning(self) -> bool:
+        """True while the time loop is still timing candidate tilings on its cycles."""
+        return lib().armon_solver_tuning(self._h) == 1
+
+    def split_pass(self) -> bool:
+        """True when the axis passes run split (face launch + cell launch), False when fused."""
+        return lib().armon_solver_split_pass(self._h) == 1
+
+
+def tiling_cache_clear() -> None:
+    """Forgets the tilings measured so far in this process (armon_tiling_cache_clear)."""
+    lib().armon_tiling_cache_clear()
 
 
 def real_cells(p: Params, a: np.ndarray) -> np.ndarray:

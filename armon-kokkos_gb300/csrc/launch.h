@@ -33,6 +33,8 @@ cudaError_t launch_sweep_batch_split(const SweepArgs<float>* doms, const int* of
                                      int block, cudaStream_t st);
 // Blocks of the split batch pass's cell half resident on one SM.
 int sweep_batch_split_blocks_per_sm(bool fp32, int scheme, int proj, int block);
+// Blocks of the split pass's cell half (sweep_cells_kernel, last pass of a cycle) resident on one SM.
+int sweep_split_blocks_per_sm(bool fp32, int scheme, int proj, int block);
 
 // Fused axis pass over many domains (sweep_batch_kernel): doms / offsets are device arrays.
 cudaError_t launch_sweep_batch(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks, int pass,

@@ -51,13 +51,27 @@ struct armon_solver {
     bool begun = false;
     int64_t partials_cap = 0;       // blocks the dt partials have room for
     int tuned_seg[2] = {0, 0};      // measured segment lengths per axis (0: the model's)
-    bool tuned = false;
+    bool tuned = false;             // the tiling measurement has been set up for this time loop
+    struct Tune {                   // the tiling measurement in progress (see start_tuning)
+        bool active = false;
+        int delay = 0;              // cycles left before the first candidate runs
+        std::vector<std::array<int, 4>> cand;   // seg X, seg Y, block, split form
+        std::vector<float> ms;      // timed cycle of each entry of seq
+        std::vector<size_t> seq;    // candidate of each measured entry: the list forwards, then the best backwards
+        bool second = false;        // the backward entries have been appended
+        size_t pos = 0;             // next entry of seq
+        bool warm = true;           // the entry's unit-cost cycle comes next, then its timed cycle
+        std::vector<cudaEvent_t> ev;
+        std::array<int, 9> key{};
+    } tune;
+    int64_t issued = 0;             // cycles issued since begin_loop
     double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
     bool ordered = true;            // longest-first dispatch of each pass's units
     uint32_t* d_order = nullptr;    // per axis: order_cap unit indices, then order_cap costs
     uint32_t* d_cost = nullptr;
     int order_cap = 0;
     bool split = false;             // each pass as a face launch and a cell launch (sweep_split.cuh)
+    bool default_split = false;     // the form before any measurement
     void* d_faces = nullptr;        // 3 * face_stride values
     int64_t face_stride = 0;
 };
@@ -104,8 +118,10 @@ int axis_blocks(const armon_solver* s, int axis)
     return s->fp32 ? s->a32.geom[axis].blocks : s->a64.geom[axis].blocks;
 }
 
-// cost / order arrays: per axis for the (cell) pass, and per axis for the face half of split passes
+// cost / order arrays: per axis for the (cell) pass, and per axis for the face half of split passes;
+// a solver that holds a face buffer can switch forms, so it keeps room for both
 int order_arrays(const armon_solver* s) { return s->split ? 4 : 2; }
+int order_arrays_held(const armon_solver* s) { return s->d_faces ? 4 : 2; }
 
 // The next passes' unit order from the costs the last passes recorded.
 int launch_order(armon_solver* s)
@@ -130,8 +146,8 @@ int prepare_order(armon_solver* s)
         cudaFree(s->d_cost);
         s->d_order = s->d_cost = nullptr;
         s->order_cap = 0;
-        cudaError_t e = cudaMalloc(&s->d_order, sizeof(uint32_t) * order_arrays(s) * (size_t)need);
-        if (e == cudaSuccess) e = cudaMalloc(&s->d_cost, sizeof(uint32_t) * order_arrays(s) * (size_t)need);
+        cudaError_t e = cudaMalloc(&s->d_order, sizeof(uint32_t) * order_arrays_held(s) * (size_t)need);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_cost, sizeof(uint32_t) * order_arrays_held(s) * (size_t)need);
         if (e != cudaSuccess) {
             set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
             return ARMON_ERR_NOMEM;
@@ -204,8 +220,9 @@ int build_graph(armon_solver* s)
     return ARMON_OK;
 }
 
-int enqueue(armon_solver* s, int n_cycles)
+int enqueue_steady(armon_solver* s, int n_cycles)
 {
+    s->issued += n_cycles;
     if (s->graph_cycles > 0 && n_cycles >= s->graph_cycles) {
         int rc = build_graph(s);
         if (rc != ARMON_OK) return rc;
@@ -244,32 +261,27 @@ int ensure_stage(armon_solver* s)
     return ARMON_OK;
 }
 
-// Tiling of a lone domain, measured.  With the GPU to itself, the best segment length depends on
-// more than the cells a thread walks (how full the last wave of blocks is, how many blocks share an
-// SM, how unevenly the units cost once wave fronts have formed, cache traffic), so begin_loop times
-// a few candidate tilings -- the model's, and segments aiming at 1, 2, 3, 4, 6 and 8 waves of
-// resident blocks, for blocks of 128 and of 32 lines unless the caller fixed the block -- keeps the
-// fastest and caches it per geometry for the process.  The candidates run real cycles from 32
-// cycles into the run, on a copy of the state that is put back afterwards, so the time loop then
-// starts from the very same state (when the device has no room for the copy they are timed on the
-// pass of cycle 0, which reads one buffer set, writes the other and leaves the step state alone).
-// Results never depend on the tiling.  Domains under 2^20 cells, single-pass splittings and a
-// caller-fixed seg_len are left to the model.
-struct Tiling {
-    int seg[2];
-    int block;
-    bool operator==(const Tiling& o) const { return seg[0] == o.seg[0] && seg[1] == o.seg[1] && block == o.block; }
-};
+// Tiling of a lone domain, measured on the caller's own cycles.  With the GPU to itself, the best
+// segment length depends on more than the cells a thread walks (how full the last wave of blocks
+// is, how many blocks share an SM, how unevenly the units cost -- fronts against fluid at rest --,
+// cache traffic), and so does the pass form (split passes keep the FP64 pipe busier where cells are
+// computed, fused ones move half the bytes where runs are streamed), so the time loop times a few
+// candidates -- the model's segments and segments aiming at 1, 2, 3, 4, 6 and 8 waves of resident
+// blocks, for each form the solver can run (a solver holding a face buffer runs both) and for
+// blocks of 128 lines (also of 32 when the caller fixed it) -- keeps the fastest and caches it per
+// geometry for the process.  Results never depend on the tiling or the form, so the candidates run
+// the loop's real cycles: after kTuneDelay cycles with the model's tiling (the fronts form), each
+// candidate runs one cycle that records its units' costs (for longest-first dispatch) and one timed
+// cycle, the list forwards, then the four fastest again backwards, so that a cost drifting with the
+// flow weighs alike on the finalists.  The loop pays only the difference between the candidates and
+// the best, a few cycles' worth.  A loop that ends before the measurement does keeps the model's
+// tiling and caches nothing.  Domains under 2^20 cells, single-pass splittings and a caller-fixed
+// seg_len are left to the model.
+using Tiling = std::array<int, 4>;   // segment length X, segment length Y, block lines, split form
 std::map<std::array<int, 9>, Tiling> g_tilings;
 std::mutex g_tilings_mu;
-
-int launch_pass0(armon_solver* s)
-{
-    cudaError_t e = launch_pass(s, 0, false);
-    if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
-    s->launches += s->split ? 2 : 1;
-    return ARMON_OK;
-}
+constexpr int kTuneDelay = 16;
+constexpr size_t kTuneFinalists = 4;
 
 int refill(armon_solver* s)
 {
@@ -293,163 +305,187 @@ int ensure_partials(armon_solver* s)
     return ARMON_OK;
 }
 
-void set_tiling(armon_solver* s, const Tiling& t)
+int apply_tiling(armon_solver* s, const Tiling& t)
 {
-    s->tuned_seg[0] = t.seg[0];
-    s->tuned_seg[1] = t.seg[1];
-    s->block = t.block;
+    s->tuned_seg[0] = t[0];
+    s->tuned_seg[1] = t[1];
+    s->block = t[2];
+    s->split = t[3] != 0 && s->d_faces != nullptr;
+    int rc = refill(s);
+    return rc != ARMON_OK ? rc : ensure_partials(s);
 }
 
-// Times each candidate tiling: on developed cycles (`cycles` > 0: one warm-up cycle that records
-// the unit costs, then `cycles` timed cycles) or on the pass of the current cycle (`cycles` == 0:
-// warm-up pass, then two timed passes).  Returns the index of the fastest in *best.
-int time_candidates(armon_solver* s, const std::vector<Tiling>& cand, int cycles, size_t* best)
+std::array<int, 9> tiling_key(const armon_solver* s)
 {
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    CUDA_TRY(cudaEventCreate(&e0));
-    CUDA_TRY(cudaEventCreate(&e1));
-    // On developed cycles the state keeps developing while the candidates run, so each is timed
-    // twice, the list forwards and then backwards, and the two times are summed: a cost that
-    // drifts linearly with the cycle then weighs the same on every candidate.
-    std::vector<float> total(cand.size(), 0.f);
-    std::vector<size_t> seq;
-    for (size_t i = 0; i < cand.size(); i++) seq.push_back(i);
-    if (cycles > 0)
-        for (size_t i = cand.size(); i-- > 0;) seq.push_back(i);
-    int rc = ARMON_OK;
-    for (size_t q = 0; q < seq.size() && rc == ARMON_OK; q++) {
-        const size_t i = seq[q];
-        set_tiling(s, cand[i]);
-        rc = refill(s);
-        if (rc == ARMON_OK) rc = ensure_partials(s);
-        if (rc == ARMON_OK) rc = cycles > 0 ? enqueue_direct(s, 1) : launch_pass0(s);
-        if (rc == ARMON_OK && cycles == 0) rc = launch_order(s);
-        if (rc == ARMON_OK && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK) {
-            if (cycles > 0) rc = enqueue_direct(s, cycles);
-            else for (int k = 0; k < 2 && rc == ARMON_OK; k++) rc = launch_pass0(s);
-        }
-        if (rc == ARMON_OK && cudaEventRecord(e1, s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        float ms = 0;
-        if (rc == ARMON_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        total[i] += ms;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    *best = size_t(std::min_element(total.begin(), total.end()) - total.begin());
-    return rc;
+    const armon_params& p = s->p;
+    return {p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting, s->o.block_lines,
+            (s->o.split_pass + 1) | (s->d_faces ? 4 : 0) | (s->o.reuse >= 0 ? 8 : 0), s->ordered ? 1 : 0};
 }
 
-// The arrays a cycle changes (rho, umat, vmat, Emat, pmat, cmat, gmat), saved so that the tiling
-// can be measured on real cycles and the time loop then restarts from the saved state bit for bit.
-constexpr int kSnapArrays[7] = {2, 3, 4, 5, 6, 7, 8};
-constexpr int kTuneWarmCycles = 32;   // cycles run before the measurement, to develop the flow
-constexpr int kTuneCycles = 2;        // timed cycles per candidate
-
-int tune_tiling(armon_solver* s)
+// the cost model's tiling in the solver's default form
+Tiling model_tiling(const armon_solver* s)
 {
+    return Tiling{0, 0, s->o.block_lines > 0 ? s->o.block_lines : 128, s->default_split ? 1 : 0};
+}
+
+void end_tuning(armon_solver* s)
+{
+    for (cudaEvent_t e : s->tune.ev) cudaEventDestroy(e);
+    s->tune = armon_solver::Tune{};
+}
+
+// Called by begin_loop: the cached tiling of this geometry, or the measurement's set-up.
+int start_tuning(armon_solver* s)
+{
+    end_tuning(s);
     if (s->tuned || s->o.seg_len > 0 || s->npass < 2) return ARMON_OK;
-    s->tuned = true;
     const armon_params& p = s->p;
     if ((int64_t)p.nx * p.ny < (1 << 20)) return ARMON_OK;
-    const std::array<int, 9> key{p.nx, p.ny, s->fp32 ? 32 : 64, p.scheme, p.projection, p.axis_splitting,
-                                 s->o.block_lines, s->split ? 1 : 0, s->ordered ? 1 : 0};
+    const std::array<int, 9> key = tiling_key(s);
     {
         std::lock_guard<std::mutex> lk(g_tilings_mu);
         auto it = g_tilings.find(key);
         if (it != g_tilings.end()) {
-            set_tiling(s, it->second);
-            int rc = refill(s);
-            return rc != ARMON_OK ? rc : ensure_partials(s);
+            s->tuned = true;
+            return apply_tiling(s, it->second);
         }
     }
-    const StepState st = *s->h_state;
-    if (!(st.status == STATUS_RUNNING && st.time < p.max_time && st.cycle < p.max_cycles)) return ARMON_OK;
-
-    // candidates per block size: the model's tiling, then segments aiming at w waves of resident
-    // blocks per axis
+    // candidates per form and block size: the model's tiling, then segments aiming at w waves of
+    // resident blocks per axis
     const int halo = stencil_reach(&p);
-    std::vector<Tiling> cand;
-    std::vector<int> blocks;
-    if (s->o.block_lines > 0) blocks.push_back(s->block); else blocks = {128, 32};
-    for (int block : blocks) {
-        const int slots = s->sm_count * sweep_blocks_per_sm(s->fp32, p.scheme, p.projection, block);
-        Tiling model{{0, 0}, block};
+    const int block = s->o.block_lines > 0 ? s->o.block_lines : 128;
+    std::vector<int> forms;
+    if (s->d_faces && s->o.split_pass == 0) forms = {1, 0}; else forms = {s->split ? 1 : 0};
+    auto& T = s->tune;
+    for (int form : forms) {
+        const int per_sm = form ? sweep_split_blocks_per_sm(s->fp32, p.scheme, p.projection, block)
+                                : sweep_blocks_per_sm(s->fp32, p.scheme, p.projection, block);
+        const int slots = s->sm_count * per_sm;
+        Tiling model{0, 0, block, form};
         for (int axis = 0; axis < 2; axis++) {
             const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
-            model.seg[axis] = choose_segments(n, nl, block, halo, s->sm_count, 0).seg_len;
+            model[axis] = choose_segments(n, nl, block, halo, s->sm_count, 0).seg_len;
         }
-        cand.push_back(model);
+        T.cand.push_back(model);
         for (int w : {1, 2, 3, 4, 6, 8}) {
-            Tiling c{{0, 0}, block};
+            Tiling c{0, 0, block, form};
             for (int axis = 0; axis < 2; axis++) {
                 const int n = axis == 0 ? p.nx : p.ny, nl = axis == 0 ? p.ny : p.nx;
                 const AxisTiling t = axis_tiling(n, nl, block, n);   // one segment: nlb, spb
                 const int per_line = std::max(1, (int)std::lround(double(w) * slots * t.spb / t.nlb));
-                c.seg[axis] = std::max(16, (n + per_line - 1) / per_line);
+                c[axis] = std::max(16, (n + per_line - 1) / per_line);
             }
-            if (std::find(cand.begin(), cand.end(), c) == cand.end()) cand.push_back(c);
+            if (std::find(T.cand.begin(), T.cand.end(), c) == T.cand.end()) T.cand.push_back(c);
         }
     }
+    for (size_t i = 0; i < T.cand.size(); i++) T.seq.push_back(i);
+    const size_t entries = T.cand.size() + std::min(kTuneFinalists, T.cand.size());
+    T.ev.assign(2 * entries, nullptr);
+    for (auto& e : T.ev) CUDA_TRY(cudaEventCreate(&e));
+    T.key = key;
+    T.delay = kTuneDelay;
+    T.pos = 0;
+    T.warm = true;
+    T.active = true;
+    return ARMON_OK;
+}
 
-    // On developed cycles when the device has room for a copy of the state, else on the pass of
-    // cycle 0.  The measured cycles run past the caller's max_cycles / max_time if need be: the
-    // copy is put back afterwards and the loop bounds with it.
-    const int need = kTuneWarmCycles + 2 * (int)cand.size() * (1 + kTuneCycles);
-    void* snap[7] = {};
-    bool developed = true;
-    const size_t bytes = (size_t)p.nb_cells * s->elem;
-    for (int k = 0; k < 7 && developed; k++)
-        if (cudaMalloc(&snap[k], bytes) != cudaSuccess) { cudaGetLastError(); developed = false; }
-    size_t best = 0;
-    int rc = ARMON_OK;
-    if (developed) {
-        const int32_t max_cycles = s->p.max_cycles;
-        const double max_time = s->p.max_time;
-        s->p.max_cycles = std::numeric_limits<int32_t>::max();
-        s->p.max_time = std::numeric_limits<double>::infinity();
-        rc = refill(s);
-        for (int k = 0; k < 7 && rc == ARMON_OK; k++)
-            if (cudaMemcpyAsync(snap[k], s->arr[kSnapArrays[k]], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
-                rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK) rc = enqueue_direct(s, kTuneWarmCycles);
-        if (rc == ARMON_OK) rc = time_candidates(s, cand, kTuneCycles, &best);
-        // valid only if every cycle ran (the loop may have reached max_time)
-        if (rc == ARMON_OK) rc = sync_state(s);
-        const StepState& now = *s->h_state;
-        const bool ran = rc == ARMON_OK && now.status == STATUS_RUNNING && now.cycle == st.cycle + need;
-        s->p.max_cycles = max_cycles;
-        s->p.max_time = max_time;
-        // restore: set 0 and p, c, g from the copy, set 1 = set 0, the step state as it was
-        for (int k = 0; k < 7 && rc == ARMON_OK; k++)
-            if (cudaMemcpyAsync(s->arr[kSnapArrays[k]], snap[k], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
-                rc = ARMON_ERR_CUDA;
-        for (int k = 0; k < 4 && rc == ARMON_OK; k++)
-            if (cudaMemcpyAsync(s->arr[11 + k], s->arr[2 + k], bytes, cudaMemcpyDeviceToDevice, s->stream) != cudaSuccess)
-                rc = ARMON_ERR_CUDA;
-        *s->h_state = st;
-        if (rc == ARMON_OK &&
-            cudaMemcpyAsync(s->d_state, s->h_state, sizeof(StepState), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
-            rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = ARMON_ERR_CUDA;
-        if (rc == ARMON_OK && !ran) developed = false;
+// The forward list has run: the finalists go again, backwards.  Returns true when it appended them.
+bool add_finalists(armon_solver* s)
+{
+    auto& T = s->tune;
+    if (T.second) return false;
+    T.second = true;
+    if (cudaEventSynchronize(T.ev[2 * T.seq.size() - 1]) != cudaSuccess) return false;
+    std::vector<std::pair<float, size_t>> fwd;
+    for (size_t q = 0; q < T.seq.size(); q++) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, T.ev[2 * q], T.ev[2 * q + 1]) != cudaSuccess) return false;
+        fwd.emplace_back(ms, T.seq[q]);
     }
-    for (void* a : snap) if (a) cudaFree(a);
-    if (rc == ARMON_OK && !developed) rc = time_candidates(s, cand, 0, &best);
-    if (rc != ARMON_OK) {
-        set_error("tiling measurement failed");
-        refill(s);
-        return rc;
+    std::sort(fwd.begin(), fwd.end());
+    const size_t nf = std::min(kTuneFinalists, fwd.size());
+    std::vector<size_t> fin;
+    for (size_t k = 0; k < nf; k++) fin.push_back(fwd[k].second);
+    std::sort(fin.begin(), fin.end());
+    for (size_t k = nf; k-- > 0;) T.seq.push_back(fin[k]);   // backwards in list order
+    return true;
+}
+
+// The finalists have run again: keep the fastest over both visits if every measured cycle ran, else
+// the model's tiling.
+int finish_tuning(armon_solver* s)
+{
+    auto& T = s->tune;
+    const size_t nc = T.cand.size();
+    std::vector<float> total(nc, 0.f);
+    std::vector<int> visits(nc, 0);
+    CUDA_TRY(cudaEventSynchronize(T.ev[2 * T.seq.size() - 1]));
+    for (size_t q = 0; q < T.seq.size(); q++) {
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, T.ev[2 * q], T.ev[2 * q + 1]));
+        total[T.seq[q]] += ms;
+        visits[T.seq[q]]++;
     }
-    set_tiling(s, cand[best]);
-    rc = refill(s);
+    int rc = sync_state(s);
     if (rc != ARMON_OK) return rc;
-    {
-        std::lock_guard<std::mutex> lk(g_tilings_mu);
-        g_tilings[key] = cand[best];
+    const StepState& st = *s->h_state;
+    const bool ran = st.status == STATUS_RUNNING && st.cycle == s->issued;
+    size_t best = 0;
+    float best_t = 0.f;
+    bool have = false;
+    for (size_t i = 0; i < nc; i++) {
+        if (visits[i] < 2) continue;
+        if (!have || total[i] < best_t) { best = i; best_t = total[i]; have = true; }
     }
-    return ensure_partials(s);
+    const Tiling choice = ran && have ? T.cand[best] : model_tiling(s);
+    const std::array<int, 9> key = T.key;
+    end_tuning(s);
+    s->tuned = ran;
+    rc = apply_tiling(s, choice);
+    if (rc == ARMON_OK && ran) {
+        std::lock_guard<std::mutex> lk(g_tilings_mu);
+        g_tilings[key] = choice;
+    }
+    return rc;
+}
+
+// n cycles of the time loop, the first ones measuring candidate tilings while a measurement runs.
+int enqueue(armon_solver* s, int n_cycles)
+{
+    auto& T = s->tune;
+    while (n_cycles > 0 && T.active) {
+        int rc = ARMON_OK;
+        if (s->issued + 1 > s->cfg.max_cycles) {   // the loop ends first: keep the model's tiling
+            end_tuning(s);
+            rc = apply_tiling(s, model_tiling(s));
+            if (rc != ARMON_OK) return rc;
+            break;
+        }
+        if (T.delay > 0) {
+            rc = enqueue_direct(s, 1);
+            T.delay--;
+        } else if (T.warm) {
+            // the candidate's first cycle records its units' costs for longest-first dispatch
+            rc = apply_tiling(s, T.cand[T.seq[T.pos]]);
+            if (rc == ARMON_OK) rc = enqueue_direct(s, 1);
+            T.warm = false;
+        } else {
+            CUDA_TRY(cudaEventRecord(T.ev[2 * T.pos], s->stream));
+            rc = enqueue_direct(s, 1);
+            if (rc == ARMON_OK) CUDA_TRY(cudaEventRecord(T.ev[2 * T.pos + 1], s->stream));
+            T.pos++;
+            T.warm = true;
+        }
+        if (rc != ARMON_OK) return rc;
+        s->issued++;
+        n_cycles--;
+        if (T.pos == T.seq.size() && !add_finalists(s)) {
+            rc = finish_tuning(s);
+            if (rc != ARMON_OK) return rc;
+        }
+    }
+    return enqueue_steady(s, n_cycles);
 }
 
 // Puts the current state back into set 0 (rho, umat, vmat, Emat) so that the reference's
@@ -550,6 +586,7 @@ static int solver_create(const armon_params* p, const armon_solver_opts* opts, d
             e = cudaSuccess;
         }
     }
+    s->default_split = s->split;
     if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state, 0, sizeof(StepState), s->stream);
     if (e != cudaSuccess) { armon_solver_destroy(s); return cuda_fail(e, "solver allocation"); }
     std::memset(s->h_state, 0, sizeof(StepState));
@@ -575,6 +612,7 @@ void armon_solver_destroy(armon_solver* s)
 {
     if (!s) return;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    end_tuning(s);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->owns_arrays)
         for (auto& a : s->arr) if (a) cudaFree(a);
@@ -618,8 +656,9 @@ int armon_solver_begin_loop(armon_solver* s)
     CUDA_TRY(launch_begin(b, s->fp32, s->sm_count * 4, s->stream));
     s->launches++;
     s->begun = true;
+    s->issued = 0;
     int rc = sync_state(s);
-    if (rc == ARMON_OK) rc = tune_tiling(s);
+    if (rc == ARMON_OK) rc = start_tuning(s);
     return rc;
 }
 
@@ -793,6 +832,16 @@ int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2])
 }
 
 int armon_solver_block_lines(const armon_solver* s) { return s->block; }
+
+int armon_solver_tuning(const armon_solver* s) { return s->tune.active ? 1 : 0; }
+
+int armon_solver_split_pass(const armon_solver* s) { return s->split ? 1 : 0; }
+
+void armon_tiling_cache_clear(void)
+{
+    std::lock_guard<std::mutex> lk(g_tilings_mu);
+    g_tilings.clear();
+}
 
 int armon_solve_host(const armon_params* p, const armon_solver_opts* opts, const double* const in[4],
                      double* const out[5], armon_params* final_state)

@@ -112,11 +112,6 @@ template <class T> constexpr int sweep_batch_cells_min_blocks() { return sizeof(
 #ifndef ARMON_SWEEP_PREFETCH
 #define ARMON_SWEEP_PREFETCH 2
 #endif
-// The same for the cell half of a split pass (sweep_split.cuh).
-#ifndef ARMON_CELLS_PREFETCH
-#define ARMON_CELLS_PREFETCH 0
-#endif
-template <class T> __host__ __device__ constexpr bool cells_prefetch() { return ((ARMON_CELLS_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return ((ARMON_SWEEP_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 
 namespace armon {
@@ -169,21 +164,14 @@ struct SweepArgs {
 
 // ---- Exact reuse over runs of identical inputs (SweepArgs::reuse) ----
 // A pass is a pure function of the cells it reads: the results at a position of the march depend
-// on a window of the positions before it, the same operations in the same order at every
-// position.  When every input in that window equals, bit for bit, the input one position earlier,
-// the results are the same bits as the previous position's, so the pass stores those instead of
-// recomputing them (fluid at rest, or any uniform state, is such a run).  Loads and stores still
-// happen for every cell.  The thresholds are the depth of each march's pipeline plus a margin: a
-// position is reused once this many consecutive positions loaded the same bits as their
-// predecessors.  Fused march: the projection of cell t - 4 depends on cells t - 8 .. t (the deepest
-// register, the advection flux of face t - 4, on t - 8 .. t - 1), so 9 equal pairs make every
-// register and result repeat.  Face half: the flux of face t - 1 depends on cells t - 3 .. t, and
-// its registers on t - 4 .. t - 1: 4 pairs.  Cell half: at step t it reads face t and cell t - 1
-// (one "unit"); the projection of cell t - 3 depends on units t - 5 .. t: 6 pairs.
-constexpr int kReuseFused = 10;
-constexpr int kReuseFaces = 5;
-constexpr int kReuseCells = 7;
-
+// on a window of positions around it, through the same operations in the same order at every
+// position.  So where a line holds a run of cells equal bit for bit (fluid at rest, or any uniform
+// state), every position whose window lies inside the run has the same results, the run's
+// "uniform" results.  Each march evaluates those once (its stage functions on operands that are
+// all the run's state), streams the run's positions -- loads compared with the run's state, then
+// stores of the uniform results -- several at a time with its pipeline registers dead, and at the
+// first position that differs restarts the pipeline from the registers a march over the run would
+// hold (the same single evaluation).  Loads and stores still happen for every cell.
 __device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
 
@@ -618,25 +606,183 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             }
             return stale;
         };
+        // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
+        const auto mirror = [&](CellIn<T>& c, int side) {
+            if (side) {
+                if (g.f_unit) {
+                    const uint32_t sh = side == 1 ? 0 : 2;
+                    c.ua = qneg_if(c.ua, (g.fneg >> sh) & 1u);
+                    c.uo = qneg_if(c.uo, (g.fneg >> (sh + 1)) & 1u);
+                } else {
+                    c.ua = c.ua * (side == 1 ? g.fa_lo : g.fa_hi);
+                    c.uo = c.uo * (side == 1 ? g.fo_lo : g.fo_hi);
+                }
+            }
+        };
+        // EOS and the products the faces share, of a loaded (non-stale) cell
+        const auto prepare = [&](CellIn<T>& c) {
+            eos(c, A.gamma, gamma_m1);
+            c.rc = qmul<1>(c.rho, c.c);
+            c.rcu = qmul<1>(c.rc, c.ua);
+            c.dm = mul_dx(c.rho, g);
+        };
+        // src/kernels/euler_projection.cpp:36-46 for a cell Lc between advection fluxes a0 and a1
+        const auto project = [&](const Lag<T>& Lc, const Adv<T>& a0, const Adv<T>& a1, T (&o)[4]) {
+            T dXr = qmul<7>(Lc.W, Lc.rho);
+            o[0] = div_dx(dXr - (a1.r - a0.r), g);
+            T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (a1.ra - a0.ra), g);
+            T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (a1.ro - a0.ro), g);
+            T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (a1.rE - a0.rE), g);
+            const auto inv_rho = qrecip_at<8>(o[0]);
+            o[1] = qdiv_at<8>(tmp_ra, inv_rho);
+            o[2] = qdiv_at<8>(tmp_ro, inv_rho);
+            o[3] = qdiv_at<8>(tmp_rE, inv_rho);
+        };
+        const auto store_out = [&](int mm, const T (&o)[4]) {
+            const int64_t idx = base + (int64_t)mm * s;
+            out[0][idx] = o[0];
+            out[axis == 0 ? 1 : 2][idx] = o[1];
+            out[axis == 0 ? 2 : 1][idx] = o[2];
+            out[3][idx] = o[3];
+        };
+        const auto add_dt = [&](const T (&o)[4], T c) {
+            // dt_CFL of the state after this pass, with c from this pass's EOS
+            if (axis == 0) acc.add(o[1], o[2], c);
+            else acc.add(o[2], o[1], c);
+        };
+        // Every register of the march as it stands after a step whose window held only cells equal
+        // to u (u prepared): the same stage functions on the same operands, each evaluated once.
+        // Registers whose window would reach before the segment's first position are never read
+        // into a result (results start at a0, whose window starts at t0), so this also stands for
+        // the march's start.
+        const auto uniform_march = [&](const CellIn<T>& c) {
+            C0 = c; C1 = c; C2 = c;
+            G2 = godunov(c, c); G1 = G2;
+            if (kGAD) { D2 = gad_diff(G2, c, c); D1 = D2; D0 = D2; }
+            Flux<T> f;
+            if (kGAD) {
+                f = gad(G2, D2, D2, D2, c.dm, c.dm, A.limiter, dt);
+            } else {
+                f.us = G2.us; f.ps = G2.ps;
+            }
+            f.psus = qmul<4>(f.ps, f.us);
+            f.dtus = qmul<4>(dt, f.us);
+            F0 = f; F1 = f; F2 = f; F3 = f; F4 = f;
+            L3 = lagrange(c, f, f, dt, dx); L2 = L3; L1 = L3;
+            if (kE2) {
+                d23 = lag_diff(L3, L3); d12 = d23; d01 = d23;
+                s23 = L3.W + L3.W; s12 = s23; s01 = s23;
+            }
+            A1 = kE2 ? advect2(f, f, f, L3, L3, d23, d23, d23, s23, s23, s23, dx) : advect1(f, L3, L3);
+            A0 = A1;
+        };
+
         // the state of the next position, loaded one iteration ahead so that the loads' latency
         // overlaps an iteration's arithmetic (ARMON_SWEEP_PREFETCH), else at the top of its iteration
         constexpr bool kPrefetch = sweep_prefetch<T>();
         T next_rho{}, next_ua{}, next_uo{}, next_E{};
-        if constexpr (kPrefetch) {
-            int m, side;
-            source(t0, m, side);
-            const int64_t i = base + (int64_t)m * s;
-            next_rho = rho_in[i]; next_ua = ua_in[i]; next_uo = uo_in[i]; next_E = E_in[i];
-        }
+        const auto prime = [&](int tt) {
+            if constexpr (kPrefetch) {
+                int m, side;
+                source(tt, m, side);
+                const int64_t i = base + (int64_t)m * s;
+                next_rho = rho_in[i]; next_ua = ua_in[i]; next_uo = uo_in[i]; next_E = E_in[i];
+            }
+        };
 
-        // the results of the last projection, for positions that reuse them
-        __shared__ T reuse_out[4][128];
-        const int tid = threadIdx.x;
+        // Exact reuse: in a run of positions whose cells equal u (bit for bit, after the mirror), a
+        // position's results equal the run's uniform results once the window of its projection
+        // (cells t - 2 H .. t) lies inside the run; such positions are streamed, kReuseBatch at a time,
+        // with the march's registers dead, and the march restarts from uniform_march(u) at the first
+        // cell that differs.  The segment's first position opens a run.
+        // The run's state (rho, ua, uo, E, p, c) and uniform results (rho, ua, uo, E) live in this
+        // thread's slot of shared memory while the march computes, so that they take no registers
+        // from the pipeline.
         const bool reuse = A.reuse != 0;
-        int run = 0;                         // equal consecutive loads ending at t (-1 after a stale one)
+        constexpr int kEnter = 2 * H;        // equal pairs that put a projection's window inside a run
+        constexpr int kReuseBatch = 4;
+        __shared__ T run_slot[10][128];
+        const int tid = threadIdx.x;
+        const auto keep_run = [&](const CellIn<T>& c, const T (&o)[4]) {
+            run_slot[0][tid] = c.rho; run_slot[1][tid] = c.ua; run_slot[2][tid] = c.uo; run_slot[3][tid] = c.E;
+            run_slot[4][tid] = c.p; run_slot[5][tid] = c.c;
+            run_slot[6][tid] = o[0]; run_slot[7][tid] = o[1]; run_slot[8][tid] = o[2]; run_slot[9][tid] = o[3];
+        };
+        int run = 0;                         // equal consecutive cells ending at t (-1 after a stale one)
+        bool counted = false;                // the run's speeds are in the dt maxima
+        // Streams the positions from t on whose cell equals the run's; returns the first that
+        // differs (t1 + 1 at the end of the segment).
+        const auto stream = [&](int t) -> int {
+            CellIn<T> u;
+            u.rho = run_slot[0][tid]; u.ua = run_slot[1][tid]; u.uo = run_slot[2][tid]; u.E = run_slot[3][tid];
+            const T up = run_slot[4][tid], uc = run_slot[5][tid];
+            const T u_out[4] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid], run_slot[9][tid]};
+            while (t <= t1) {
+                const int nb = min(kReuseBatch, t1 - t + 1);
+                bool same[kReuseBatch];
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) {
+                    same[q] = false;
+                    if (q < nb) {
+                        int m, side;
+                        const bool stale = source(t + q, m, side);
+                        const int64_t idx = base + (int64_t)m * s;
+                        CellIn<T> c;
+                        c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                        mirror(c, side);
+                        same[q] = !stale && same_state(c, u);
+                    }
+                }
+                int k = 0;
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) k += (k == q && same[q]) ? 1 : 0;
+                for (int q = 0; q < k; q++) {
+                    const int tt = t + q;
+                    if (tt >= a0 && tt < b0 && (LAST || A.write_eos)) {   // owned real cell
+                        const int64_t idx = base + (int64_t)tt * s;
+                        A.pmat[idx] = up;
+                        A.cmat[idx] = uc;
+                        A.gmat[idx] = (1 + A.gamma) / 2;
+                    }
+                    if (tt - H >= a0) {
+                        store_out(tt - H, u_out);
+                        if (LAST && !counted) { add_dt(u_out, uc); counted = true; }
+                    }
+                }
+                t += k;
+                if (k < nb) break;
+            }
+            return t;
+        };
+        // the march resumes as if every cell before the current position were the run's
+        const auto restart = [&]() {
+            CellIn<T> u;
+            u.rho = run_slot[0][tid]; u.ua = run_slot[1][tid]; u.uo = run_slot[2][tid]; u.E = run_slot[3][tid];
+            prepare(u);
+            uniform_march(u);
+        };
 
+        int t = t0;
+        if (reuse) {
+            int m, side;
+            const bool stale = source(t0, m, side);
+            if (!stale) {
+                const int64_t idx = base + (int64_t)m * s;
+                CellIn<T> c;
+                c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                mirror(c, side);
+                prepare(c);
+                uniform_march(c);
+                T o[4];
+                project(kE2 ? L1 : L2, A0, A1, o);
+                keep_run(c, o);
+                t = stream(t0 + 1);
+                if (t <= t1) restart();
+            }
+        }
+        prime(t);
 #pragma unroll kSweepUnroll
-        for (int t = t0; t <= t1; ++t) {
+        for (; t <= t1; ++t) {
             // ---- load cell t (real, mirrored ghost, or untouched ghost) + EOS ----
             {
                 CellIn<T> c;
@@ -648,59 +794,30 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                     c.ua = next_ua;
                     c.uo = next_uo;
                     c.E = next_E;
-                    int m1, side1;
-                    source(min(t + 1, t1), m1, side1);
-                    const int64_t i1 = base + (int64_t)m1 * s;
-                    next_rho = rho_in[i1]; next_ua = ua_in[i1]; next_uo = uo_in[i1]; next_E = E_in[i1];
+                    prime(min(t + 1, t1));
                 } else {
                     c.rho = rho_in[idx];
                     c.ua = ua_in[idx];
                     c.uo = uo_in[idx];
                     c.E = E_in[idx];
                 }
-                if (side) {
-                    // boundary_conditions: umat * u_factor, vmat * v_factor (+-1: a sign flip)
-                    if (g.f_unit) {
-                        const uint32_t sh = side == 1 ? 0 : 2;
-                        c.ua = qneg_if(c.ua, (g.fneg >> sh) & 1u);
-                        c.uo = qneg_if(c.uo, (g.fneg >> (sh + 1)) & 1u);
-                    } else {
-                        c.ua = c.ua * (side == 1 ? g.fa_lo : g.fa_hi);
-                        c.uo = c.uo * (side == 1 ? g.fo_lo : g.fo_hi);
-                    }
-                }
-                if (reuse) {
-                    run = stale ? -1 : (t > t0 && same_state(c, C2)) ? run + 1 : 0;
-                    if (run >= kReuseFused) {
-                        // every register and result of this step equals the previous step's
-                        if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {
-                            A.pmat[idx] = C2.p;
-                            A.cmat[idx] = C2.c;
-                            A.gmat[idx] = (1 + A.gamma) / 2;
-                        }
-                        const int64_t o = base + (int64_t)(t - H) * s;
-                        out[0][o] = reuse_out[0][tid];
-                        out[axis == 0 ? 1 : 2][o] = reuse_out[1][tid];
-                        out[axis == 0 ? 2 : 1][o] = reuse_out[2][tid];
-                        out[3][o] = reuse_out[3][tid];
-                        continue;
-                    }
-                }
+                mirror(c, side);
+                if (reuse) run = stale ? -1 : (t > t0 && same_state(c, C2)) ? run + 1 : 0;
                 C0 = C1; C1 = C2;
                 if (stale) {
                     c.p = A.pmat[idx];
                     c.c = A.cmat[idx];
+                    c.rc = qmul<1>(c.rho, c.c);
+                    c.rcu = qmul<1>(c.rc, c.ua);
+                    c.dm = mul_dx(c.rho, g);
                 } else {
-                    eos(c, A.gamma, gamma_m1);
+                    prepare(c);
                     if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
                         A.pmat[idx] = c.p;
                         A.cmat[idx] = c.c;
                         A.gmat[idx] = (1 + A.gamma) / 2;
                     }
                 }
-                c.rc = qmul<1>(c.rho, c.c);
-                c.rcu = qmul<1>(c.rc, c.ua);
-                c.dm = mul_dx(c.rho, g);
                 C2 = c;
             }
             // ---- Godunov face t ----
@@ -742,30 +859,20 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             const int mm = k - 1;
             if (mm >= a0) {
                 const Lag<T>& Lc = kE2 ? L1 : L2;
-                // src/kernels/euler_projection.cpp:36-46
-                T dXr = qmul<7>(Lc.W, Lc.rho);
-                T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
-                T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (A1.ra - A0.ra), g);
-                T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (A1.ro - A0.ro), g);
-                T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (A1.rE - A0.rE), g);
-                const auto inv_rho = qrecip_at<8>(tmp_rho);
-                T ua = qdiv_at<8>(tmp_ra, inv_rho), uo = qdiv_at<8>(tmp_ro, inv_rho), E = qdiv_at<8>(tmp_rE, inv_rho);
-                const int64_t idx = base + (int64_t)mm * s;
-                out[0][idx] = tmp_rho;
-                out[axis == 0 ? 1 : 2][idx] = ua;
-                out[axis == 0 ? 2 : 1][idx] = uo;
-                out[3][idx] = E;
-                if (reuse) {
-                    reuse_out[0][tid] = tmp_rho;
-                    reuse_out[1][tid] = ua;
-                    reuse_out[2][tid] = uo;
-                    reuse_out[3][tid] = E;
-                }
-                if (LAST) {
-                    // dt_CFL of the state after this pass, with c from this pass's EOS (a reused
-                    // position adds the same speeds again, which leaves the maxima as they are)
-                    if (axis == 0) acc.add(ua, uo, Lc.c);
-                    else acc.add(uo, ua, Lc.c);
+                T o[4];
+                project(Lc, A0, A1, o);
+                store_out(mm, o);
+                if (LAST) add_dt(o, Lc.c);
+                if (reuse && run >= kEnter) {
+                    // cells t - 2 H .. t are equal: the following positions of the run are streamed
+                    keep_run(C2, o);
+                    counted = true;
+                    const int tn = stream(t + 1);
+                    if (tn > t1) break;
+                    restart();
+                    prime(tn);
+                    run = 0;
+                    t = tn - 1;          // the loop's increment brings it to tn
                 }
             }
         }

@@ -71,7 +71,26 @@ int batch_split_blocks_per_sm_t(int scheme, int proj, int block)
     return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
+template <class T>
+int split_blocks_per_sm_t(int scheme, int proj, int block)
+{
+    int n = 0;
+    cudaError_t e;
+    if (scheme == 1)
+        e = proj == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_cells_kernel<T, 1, 2, true>, block, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_cells_kernel<T, 1, 1, true>, block, 0);
+    else
+        e = proj == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_cells_kernel<T, 0, 2, true>, block, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sweep_cells_kernel<T, 0, 1, true>, block, 0);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
 }  // namespace
+
+int sweep_split_blocks_per_sm(bool fp32, int scheme, int proj, int block)
+{
+    return fp32 ? split_blocks_per_sm_t<float>(scheme, proj, block) : split_blocks_per_sm_t<double>(scheme, proj, block);
+}
 
 cudaError_t launch_sweep_batch_split(const SweepArgs<double>* doms, const int* offsets, int ndom, int total_blocks,
                                      int pass, BatchOrder faces, BatchOrder cells, int scheme, int proj, bool last,

@@ -121,48 +121,138 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         CellIn<T> C0{}, C1{}, C2{};
         God<T> G1{}, G2{};
         GadDiff<T> D0{}, D1{}, D2{};
-        // the last face stored, for positions that reuse it (sweep.cuh: exact reuse)
-        __shared__ T reuse_f[3][128];
-        const int tid = threadIdx.x;
+        constexpr int LAGF = kGAD ? 1 : 0;          // step t stores face t - LAGF
+        const auto prepare = [&](CellIn<T>& c) {
+            eos(c, A.gamma, gamma_m1);
+            c.rc = qmul<1>(c.rho, c.c);
+            c.rcu = qmul<1>(c.rc, c.ua);
+            c.dm = mul_dx(c.rho, g);
+        };
+        const auto flux = [&](const God<T>& Gc, const GadDiff<T>& Dm1, const GadDiff<T>& D0_, const GadDiff<T>& Dp1,
+                              T dm_l, T dm_r, const God<T>& Gr, T (&o)[3]) {
+            Flux<T> f;
+            if (kGAD) {
+                f = gad<T, MULS, ADDS>(Gc, Dm1, D0_, Dp1, dm_l, dm_r, A.limiter, dt);
+            } else {
+                f.us = Gr.us; f.ps = Gr.ps;
+            }
+            o[0] = f.us;
+            o[1] = f.ps;
+            o[2] = qmul<4>(f.ps, f.us);
+        };
+        const auto store_face = [&](int f, const T (&o)[3]) {
+            const int64_t fi = face_index(g, f, P.line);
+            us_out[fi] = o[0];
+            ps_out[fi] = o[1];
+            psus_out[fi] = o[2];
+        };
+        // the registers after a step whose window held only cells equal to u (sweep.cuh: exact reuse)
+        const auto uniform_march = [&](const CellIn<T>& c) {
+            C0 = c; C1 = c; C2 = c;
+            G2 = godunov<T, ADDS>(c, c); G1 = G2;
+            if (kGAD) { D2 = gad_diff<T, ADDS>(G2, c, c); D1 = D2; D0 = D2; }
+        };
+        const auto pcg = [&](int tt, const CellIn<T>& c) {
+            if (tt >= a0 && tt < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
+                const int64_t idx = base + (int64_t)tt * g.s;
+                A.pmat[idx] = c.p;
+                A.cmat[idx] = c.c;
+                A.gmat[idx] = (1 + A.gamma) / 2;
+            }
+        };
+
+        // Exact reuse (sweep.cuh): a face whose flux window (cells f - 2 .. f + 1 with GAD, f - 1 .. f
+        // with Godunov) lies in a run of cells equal to u gets the run's uniform flux; such positions
+        // are streamed, kReuseBatch at a time, and the march restarts from uniform_march(u).
         const bool reuse = A.reuse != 0;
+        constexpr int kEnter = kGAD ? 3 : 1;
+        constexpr int kReuseBatch = 4;
+        // the run's state (rho, ua, uo, E, p, c) and uniform face (u*, p*, p* u*), kept in this
+        // thread's slot of shared memory while the march computes
+        __shared__ T run_slot[9][128];
+        const int tid = threadIdx.x;
+        const auto keep_run = [&](const CellIn<T>& c, const T (&o)[3]) {
+            run_slot[0][tid] = c.rho; run_slot[1][tid] = c.ua; run_slot[2][tid] = c.uo; run_slot[3][tid] = c.E;
+            run_slot[4][tid] = c.p; run_slot[5][tid] = c.c;
+            run_slot[6][tid] = o[0]; run_slot[7][tid] = o[1]; run_slot[8][tid] = o[2];
+        };
+        const auto run_cell = [&]() {
+            CellIn<T> u;
+            u.rho = run_slot[0][tid]; u.ua = run_slot[1][tid]; u.uo = run_slot[2][tid]; u.E = run_slot[3][tid];
+            u.p = run_slot[4][tid]; u.c = run_slot[5][tid];
+            return u;
+        };
+        // streams the positions from t on whose cell equals the run's; returns the first that differs
+        const auto stream = [&](int t) -> int {
+            const CellIn<T> u = run_cell();
+            const T u_out[3] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid]};
+            while (t <= t1) {
+                const int nb = min(kReuseBatch, t1 - t + 1);
+                bool same[kReuseBatch];
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) {
+                    same[q] = false;
+                    if (q < nb) {
+                        CellIn<T> c;
+                        int m;
+                        int64_t idx;
+                        const bool stale = load_position(g, n, sw, base, t + q, rho_in, ua_in, uo_in, E_in, c, m, idx);
+                        same[q] = !stale && same_state(c, u);
+                    }
+                }
+                int k = 0;
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) k += (k == q && same[q]) ? 1 : 0;
+                for (int q = 0; q < k; q++) {
+                    pcg(t + q, u);
+                    if (t + q >= t0 + 1 + 2 * LAGF) store_face(t + q - LAGF, u_out);
+                }
+                t += k;
+                if (k < nb) break;
+            }
+            return t;
+        };
+        const auto restart = [&]() {
+            CellIn<T> u = run_cell();
+            prepare(u);
+            uniform_march(u);
+        };
+
+        int t = t0;
         int run = 0;
+        if (reuse) {
+            CellIn<T> c;
+            int m;
+            int64_t idx;
+            if (!load_position(g, n, sw, base, t0, rho_in, ua_in, uo_in, E_in, c, m, idx)) {
+                prepare(c);
+                uniform_march(c);
+                T o[3];
+                flux(G1, D0, D1, D2, C0.dm, C1.dm, G2, o);
+                keep_run(c, o);
+                t = stream(t0 + 1);
+                if (t <= t1) restart();
+            }
+        }
 #pragma unroll 1
-        for (int t = t0; t <= t1; ++t) {
+        for (; t <= t1; ++t) {
             {
                 CellIn<T> c;
                 int m;
                 int64_t idx;
                 const bool stale = load_position(g, n, sw, base, t, rho_in, ua_in, uo_in, E_in, c, m, idx);
-                if (reuse) {
-                    run = stale ? -1 : (t > t0 && same_state(c, C2)) ? run + 1 : 0;
-                    if (run >= kReuseFaces) {
-                        if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {
-                            A.pmat[idx] = C2.p;
-                            A.cmat[idx] = C2.c;
-                            A.gmat[idx] = (1 + A.gamma) / 2;
-                        }
-                        const int64_t fi = face_index(g, kGAD ? t - 1 : t, P.line);
-                        us_out[fi] = reuse_f[0][tid];
-                        ps_out[fi] = reuse_f[1][tid];
-                        psus_out[fi] = reuse_f[2][tid];
-                        continue;
-                    }
-                }
+                if (reuse) run = stale ? -1 : (t > t0 && same_state(c, C2)) ? run + 1 : 0;
                 C0 = C1; C1 = C2;
                 if (stale) {
                     c.p = A.pmat[idx];
                     c.c = A.cmat[idx];
+                    c.rc = qmul<1>(c.rho, c.c);
+                    c.rcu = qmul<1>(c.rc, c.ua);
+                    c.dm = mul_dx(c.rho, g);
                 } else {
-                    eos(c, A.gamma, gamma_m1);
-                    if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
-                        A.pmat[idx] = c.p;
-                        A.cmat[idx] = c.c;
-                        A.gmat[idx] = (1 + A.gamma) / 2;
-                    }
+                    prepare(c);
+                    if (m == t) pcg(t, c);
                 }
-                c.rc = qmul<1>(c.rho, c.c);
-                c.rcu = qmul<1>(c.rc, c.ua);
-                c.dm = mul_dx(c.rho, g);
                 C2 = c;
             }
             if (t >= t0 + 1) {
@@ -170,22 +260,18 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
                 G2 = godunov<T, ADDS>(C1, C2);
                 if (kGAD) { D0 = D1; D1 = D2; D2 = gad_diff<T, ADDS>(G2, C1, C2); }
             }
-            if (kGAD ? (t >= t0 + 3) : (t >= t0 + 1)) {
-                Flux<T> f;
-                if (kGAD) {
-                    f = gad<T, MULS, ADDS>(G1, D0, D1, D2, C0.dm, C1.dm, A.limiter, dt);
-                } else {
-                    f.us = G2.us; f.ps = G2.ps;
-                }
-                const int64_t fi = face_index(g, kGAD ? t - 1 : t, P.line);
-                const T psus = qmul<4>(f.ps, f.us);
-                us_out[fi] = f.us;
-                ps_out[fi] = f.ps;
-                psus_out[fi] = psus;
-                if (reuse) {
-                    reuse_f[0][tid] = f.us;
-                    reuse_f[1][tid] = f.ps;
-                    reuse_f[2][tid] = psus;
+            if (t >= t0 + 1 + 2 * LAGF) {
+                T o[3];
+                flux(G1, D0, D1, D2, C0.dm, C1.dm, G2, o);
+                store_face(t - LAGF, o);
+                if (reuse && run >= kEnter) {
+                    // the window of this face lies in a run of equal cells: stream the run
+                    keep_run(C2, o);
+                    const int tn = stream(t + 1);
+                    if (tn > t1) break;
+                    restart();
+                    run = 0;
+                    t = tn - 1;          // the loop's increment brings it to tn
                 }
             }
         }
@@ -247,80 +333,166 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
         Adv<T> d01{}, d12{}, d23{};
         T s01{}, s12{}, s23{};
         Adv<T> A0{}, A1{};
-        // face t and cell t - 1 of the next iteration, loaded one iteration ahead (ARMON_CELLS_PREFETCH)
-        constexpr bool kPrefetch = cells_prefetch<T>();
-        Flux<T> next_f{};
-        CellIn<T> next_c{};
-        if constexpr (kPrefetch) {
-            const int64_t fi = face_index(g, t0, P.line);
-            next_f.us = us_in[fi];
-            next_f.ps = ps_in[fi];
-            next_f.psus = psus_in[fi];
-        }
 
-        // the last projection's results, and the state of the cell read one step earlier, for
-        // positions that reuse them (sweep.cuh: exact reuse; a step's inputs are face t and cell t - 1)
-        __shared__ T reuse_out[4][128];
-        __shared__ T prev_cell[4][128];
-        const int tid = threadIdx.x;
+        // The inputs of step t ("unit" t): face t and the state of cell t - 1.
+        struct Unit { Flux<T> f; CellIn<T> c; };
+        const auto load_face = [&](int tt, Flux<T>& f) {
+            const int64_t fi = face_index(g, tt, P.line);
+            f.us = us_in[fi];
+            f.ps = ps_in[fi];
+            f.psus = psus_in[fi];
+        };
+        const auto load_cell = [&](int tt, CellIn<T>& c) {
+            int m;
+            int64_t idx;
+            load_position(g, n, sw, base, tt, rho_in, ua_in, uo_in, E_in, c, m, idx);
+        };
+        const auto same_unit = [&](const Flux<T>& f, const CellIn<T>& c, const Unit& v) {
+            return same_bits(f.us, v.f.us) & same_bits(f.ps, v.f.ps) & same_bits(f.psus, v.f.psus) & same_state(c, v.c);
+        };
+        const auto lagrange_of = [&](CellIn<T> c, const Flux<T>& fl, const Flux<T>& fr) {
+            c.dm = mul_dx(c.rho, g);
+            c.c = T(0);
+            return lagrange(c, fl, fr, dt, dx);
+        };
+        // src/kernels/euler_projection.cpp:36-46 for a cell Lc between advection fluxes a0 and a1
+        const auto project = [&](const Lag<T>& Lc, const Adv<T>& a0_, const Adv<T>& a1_, T (&o)[4]) {
+            T dXr = qmul<7>(Lc.W, Lc.rho);
+            o[0] = div_dx(dXr - (a1_.r - a0_.r), g);
+            T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (a1_.ra - a0_.ra), g);
+            T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (a1_.ro - a0_.ro), g);
+            T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (a1_.rE - a0_.rE), g);
+            const auto inv_rho = qrecip_at<8>(o[0]);
+            o[1] = qdiv_at<8>(tmp_ra, inv_rho);
+            o[2] = qdiv_at<8>(tmp_ro, inv_rho);
+            o[3] = qdiv_at<8>(tmp_rE, inv_rho);
+        };
+        const auto store_out = [&](int mm, const T (&o)[4]) {
+            const int64_t idx = base + (int64_t)mm * s;
+            out[0][idx] = o[0];
+            out[axis == 0 ? 1 : 2][idx] = o[1];
+            out[axis == 0 ? 2 : 1][idx] = o[2];
+            out[3][idx] = o[3];
+        };
+        // dt_CFL of the state after this pass, with c from this pass's EOS (the face half stored it
+        // for every real cell)
+        const auto add_dt = [&](int mm, const T (&o)[4]) {
+            const T c = A.cmat[base + (int64_t)mm * s];
+            if (axis == 0) acc.add(o[1], o[2], c);
+            else acc.add(o[2], o[1], c);
+        };
+        // the registers after a step whose window held only units equal to v (sweep.cuh: exact reuse)
+        const auto uniform_march = [&](const Unit& v) {
+            Flux<T> f = v.f;
+            f.dtus = qmul<4>(dt, f.us);
+            F1 = f; F2 = f; F3 = f; F4 = f;
+            L3 = lagrange_of(v.c, f, f); L2 = L3; L1 = L3;
+            if (kE2) {
+                d23 = lag_diff(L3, L3); d12 = d23; d01 = d23;
+                s23 = L3.W + L3.W; s12 = s23; s01 = s23;
+            }
+            A1 = kE2 ? advect2(f, f, f, L3, L3, d23, d23, d23, s23, s23, s23, dx) : advect1(f, L3, L3);
+            A0 = A1;
+        };
+
+        // Exact reuse (sweep.cuh): the projection of cell t - LAG_A - 1 depends on units
+        // t - 2 LAG_A - 1 .. t; positions whose window lies in a run of units equal to v are
+        // streamed, kReuseBatch at a time, and the march restarts from uniform_march(v).  The
+        // segment's run starts at unit t0 + 1 (face t0 + 1, cell t0) when face t0 equals face t0 + 1
+        // (the march's first Lagrange cell is t0, which reads faces t0 and t0 + 1).
         const bool reuse = A.reuse != 0;
-        int run = 0;
+        constexpr int kEnter = 2 * LAG_A + 1;
+        constexpr int kReuseBatch = 4;
+        // the run's unit (u*, p*, p* u*, rho, ua, uo, E) and uniform results (rho, ua, uo, E) in this
+        // thread's slot of shared memory while the march computes; slots 11..14 hold the cell of the
+        // previous step, which the next step compares with its own
+        __shared__ T run_slot[15][128];
+        const int tid = threadIdx.x;
+        const auto keep_run = [&](const Flux<T>& f, const T (&o)[4]) {
+            run_slot[0][tid] = f.us; run_slot[1][tid] = f.ps; run_slot[2][tid] = f.psus;
+            for (int q = 0; q < 4; q++) run_slot[3 + q][tid] = run_slot[11 + q][tid];
+            for (int q = 0; q < 4; q++) run_slot[7 + q][tid] = o[q];
+        };
+        const auto run_unit = [&]() {
+            Unit v;
+            v.f.us = run_slot[0][tid]; v.f.ps = run_slot[1][tid]; v.f.psus = run_slot[2][tid];
+            v.c.rho = run_slot[3][tid]; v.c.ua = run_slot[4][tid]; v.c.uo = run_slot[5][tid]; v.c.E = run_slot[6][tid];
+            return v;
+        };
+        bool counted = false;
+        // streams the positions from t on whose unit equals the run's; returns the first that differs
+        const auto stream = [&](int t) -> int {
+            const Unit v = run_unit();
+            const T v_out[4] = {run_slot[7][tid], run_slot[8][tid], run_slot[9][tid], run_slot[10][tid]};
+            while (t <= t1) {
+                const int nb = min(kReuseBatch, t1 - t + 1);
+                bool same[kReuseBatch];
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) {
+                    same[q] = false;
+                    if (q < nb) {
+                        Flux<T> f;
+                        CellIn<T> c;
+                        load_face(t + q, f);
+                        load_cell(t + q - 1, c);
+                        same[q] = same_unit(f, c, v);
+                    }
+                }
+                int k = 0;
+#pragma unroll
+                for (int q = 0; q < kReuseBatch; q++) k += (k == q && same[q]) ? 1 : 0;
+                for (int q = 0; q < k; q++) {
+                    const int mm = t + q - LAG_A - 1;
+                    if (mm >= a0) {
+                        store_out(mm, v_out);
+                        if (LAST && !counted) { add_dt(mm, v_out); counted = true; }
+                    }
+                }
+                t += k;
+                if (k < nb) break;
+            }
+            return t;
+        };
 
+        int t = t0;
+        int run = 0;
+        if (reuse) {
+            Flux<T> f0, f1;
+            CellIn<T> c;
+            load_face(t0, f0);
+            load_face(t0 + 1, f1);
+            load_cell(t0, c);
+            if (same_bits(f0.us, f1.us) & same_bits(f0.ps, f1.ps) & same_bits(f0.psus, f1.psus)) {
+                const Unit v{f1, c};
+                uniform_march(v);
+                T o[4];
+                project(kE2 ? L1 : L2, A0, A1, o);
+                run_slot[11][tid] = c.rho; run_slot[12][tid] = c.ua; run_slot[13][tid] = c.uo; run_slot[14][tid] = c.E;
+                keep_run(f1, o);
+                t = stream(t0 + 2);
+                if (t <= t1) uniform_march(run_unit());
+            }
+        }
 #pragma unroll 1
-        for (int t = t0; t <= t1; ++t) {
+        for (; t <= t1; ++t) {
             // ---- flux of face t, state of cell t - 1 ----
             Flux<T> f;
-            if constexpr (kPrefetch) {
-                f = next_f;
-                const int64_t fi = face_index(g, min(t + 1, t1), P.line);
-                next_f.us = us_in[fi];
-                next_f.ps = ps_in[fi];
-                next_f.psus = psus_in[fi];
-            } else {
-                const int64_t fi = face_index(g, t, P.line);
-                f.us = us_in[fi];
-                f.ps = ps_in[fi];
-                f.psus = psus_in[fi];
-            }
-            CellIn<T> c = next_c;
-            if constexpr (kPrefetch) {
-                // positions up to t1 - 1, the last cell the segment updates, stay inside the ghost band
-                int m;
-                int64_t idx;
-                load_position(g, n, sw, base, min(t, t1 - 1), rho_in, ua_in, uo_in, E_in, next_c, m, idx);
-            } else if (t >= t0 + 1) {
-                int m;
-                int64_t idx;
-                load_position(g, n, sw, base, t - 1, rho_in, ua_in, uo_in, E_in, c, m, idx);
-            }
-            if (reuse && t >= t0 + 1) {
-                const bool same = t >= t0 + 2 && same_bits(f.us, F4.us) && same_bits(f.ps, F4.ps) &&
-                                  same_bits(f.psus, F4.psus) && same_bits(c.rho, prev_cell[0][tid]) &&
-                                  same_bits(c.ua, prev_cell[1][tid]) && same_bits(c.uo, prev_cell[2][tid]) &&
-                                  same_bits(c.E, prev_cell[3][tid]);
-                run = same ? run + 1 : 0;
-                if (run >= kReuseCells) {
-                    const int64_t o = base + (int64_t)(t - LAG_A - 1) * s;
-                    out[0][o] = reuse_out[0][tid];
-                    out[axis == 0 ? 1 : 2][o] = reuse_out[1][tid];
-                    out[axis == 0 ? 2 : 1][o] = reuse_out[2][tid];
-                    out[3][o] = reuse_out[3][tid];
-                    continue;
-                }
-                prev_cell[0][tid] = c.rho;
-                prev_cell[1][tid] = c.ua;
-                prev_cell[2][tid] = c.uo;
-                prev_cell[3][tid] = c.E;
+            load_face(t, f);
+            CellIn<T> c{};
+            if (t >= t0 + 1) load_cell(t - 1, c);
+            if (reuse) {
+                run = (t >= t0 + 2 && same_bits(f.us, F4.us) && same_bits(f.ps, F4.ps) && same_bits(f.psus, F4.psus) &&
+                       same_bits(c.rho, run_slot[11][tid]) && same_bits(c.ua, run_slot[12][tid]) &&
+                       same_bits(c.uo, run_slot[13][tid]) && same_bits(c.E, run_slot[14][tid])) ? run + 1 : 0;
+                run_slot[11][tid] = c.rho; run_slot[12][tid] = c.ua; run_slot[13][tid] = c.uo; run_slot[14][tid] = c.E;
             }
             F1 = F2; F2 = F3; F3 = F4;
             f.dtus = qmul<4>(dt, f.us);
             F4 = f;
             // ---- Lagrange update of cell j = t - 1 ----
             if (t >= t0 + 1) {
-                c.dm = mul_dx(c.rho, g);
-                c.c = T(0);
                 L1 = L2; L2 = L3;
-                L3 = lagrange(c, F3, F4, dt, dx);
+                L3 = lagrange_of(c, F3, F4);
                 if (kE2) {
                     d01 = d12; d12 = d23; d23 = lag_diff(L2, L3);
                     s01 = s12; s12 = s23; s23 = L2.W + L3.W;
@@ -335,32 +507,21 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
             // ---- projection of cell mm = k - 1 ----
             const int mm = k - 1;
             if (mm >= a0) {
-                const Lag<T>& Lc = kE2 ? L1 : L2;
-                // src/kernels/euler_projection.cpp:36-46
-                T dXr = qmul<7>(Lc.W, Lc.rho);
-                T tmp_rho = div_dx(dXr - (A1.r - A0.r), g);
-                T tmp_ra = div_dx(qmul<7>(dXr, Lc.ua) - (A1.ra - A0.ra), g);
-                T tmp_ro = div_dx(qmul<7>(dXr, Lc.uo) - (A1.ro - A0.ro), g);
-                T tmp_rE = div_dx(qmul<7>(dXr, Lc.E) - (A1.rE - A0.rE), g);
-                const auto inv_rho = qrecip_at<8>(tmp_rho);
-                T ua = qdiv_at<8>(tmp_ra, inv_rho), uo = qdiv_at<8>(tmp_ro, inv_rho), E = qdiv_at<8>(tmp_rE, inv_rho);
-                const int64_t idx = base + (int64_t)mm * s;
-                out[0][idx] = tmp_rho;
-                out[axis == 0 ? 1 : 2][idx] = ua;
-                out[axis == 0 ? 2 : 1][idx] = uo;
-                out[3][idx] = E;
-                if (reuse) {
-                    reuse_out[0][tid] = tmp_rho;
-                    reuse_out[1][tid] = ua;
-                    reuse_out[2][tid] = uo;
-                    reuse_out[3][tid] = E;
-                }
-                if (LAST) {
-                    // dt_CFL of the state after this pass, with c from this pass's EOS (the face half
-                    // stored it for every real cell; a reused position would add the same speeds again)
-                    const T c = A.cmat[idx];
-                    if (axis == 0) acc.add(ua, uo, c);
-                    else acc.add(uo, ua, c);
+                T o[4];
+                project(kE2 ? L1 : L2, A0, A1, o);
+                store_out(mm, o);
+                if (LAST) add_dt(mm, o);
+                if (reuse && run >= kEnter) {
+                    // units t - 2 LAG_A - 1 .. t are equal: the following positions of the run are streamed
+                    keep_run(F4, o);
+                    counted = true;
+                    const int tn = stream(t + 1);
+                    if (tn > t1) break;
+                    uniform_march(run_unit());
+                    // the cell compared with the next step's: the run's
+                    for (int q = 0; q < 4; q++) run_slot[11 + q][tid] = run_slot[3 + q][tid];
+                    run = 0;
+                    t = tn - 1;          // the loop's increment brings it to tn
                 }
             }
         }

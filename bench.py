@@ -1,17 +1,26 @@
 #!/usr/bin/env python
-"""Benchmark of the Armon time step on GB300: cell-updates/s of the fused FP64 solver.
+"""Benchmark of the Armon time step on GB300: cell-updates/s.
 
 Workload (the single-domain drop-in case): circular Sod on [0,1]^2, 4096 x 4096 real cells, 5 ghost
 layers, FP64, gamma 1.4, rho/p = 1/1 inside radius 0.2 and 0.125/0.1 outside, GAD acoustic fluxes
-with the minmod limiter, second-order Euler remap, Sequential X/Y splitting, CFL 0.6.  A step is one
-solver cycle (dt reduction + X pass + Y pass) over the whole grid; the state (4 x 135 MB per buffer
-set) is larger than L2, so no flush is needed between steps.
+with the minmod limiter, second-order Euler remap, Sequential X/Y splitting, CFL 0.6, 200 cycles.
+A step is one solver cycle (dt reduction + X pass + Y pass) over the whole grid.  The timed steps
+are the last K cycles of the 200-cycle run (its most expensive part: the fronts are widest); the
+whole run's rate is reported beside them.  The state (4 x 135 MB per buffer set) is larger than
+L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
---impl reference times the reference's CPU path (the oracle's OpenMP build with the reference's
-Release flags) on the host cores.  N > 1 runs N independent replicas (one per GPU), weak scaling.
-Prints one JSON line (rank 0).
+One JSON line (rank 0).  Beside the headline it holds, at N = 1: `parity` (the GPU run against the
+strict oracle, field by field and dt cycle by cycle), `e2e` (the whole solve through the C ABI
+with host buffers; `e2e_cold` the same in a process that has not measured this geometry's tiling),
+`cpu_baseline` (the reference's own sources, Release flags, OpenMP on the host cores), and compact
+runs of the other configurations: `fp32` (8192^2 FP32 variant, with its accuracy), `batch` (the
+256-domain mix, batched against the plain path) and `serve` (a Poisson request trace).
+
+--impl reference times the reference's own time loop (its sources compiled against the project's
+Kokkos API shim with its Release flags, OpenMP) on the host cores.  N > 1 runs N independent
+replicas (one per GPU), weak scaling.
 """
 from __future__ import annotations
 
@@ -34,14 +43,16 @@ METRIC = "cell-updates/s"
 WORKLOAD = dict(test="Sod_circ", scheme="GAD", projection="euler_2nd", limiter="Minmod", splitting="Sequential",
                 nghost=5, nx=4096, ny=4096, cfl=0.6, max_time=1e9, test_option=0.04)
 BYTES_PER_CELL_UPDATE = 64          # read + write rho, u, v, E once per cycle (FP64)
+PARITY_FIELDS = ("rho", "umat", "vmat", "Emat", "pmat")
 
 
-def config(nx: int, ny: int, n: int, precision: int = 64) -> dict:
+def config(nx: int, ny: int, n: int, precision: int = 64, cycles: int = 200) -> dict:
     prec = "FP64" if precision == 64 else "FP32 storage and arithmetic, FP64 dt and conservation sums"
     esize = 8 if precision == 64 else 4
-    return {"workload": f"Sod_circ {nx}x{ny} {prec}, GAD-minmod + euler_2nd, CFL 0.6, radius 0.2, Sequential splitting",
+    return {"workload": f"Sod_circ {nx}x{ny} {prec}, GAD-minmod + euler_2nd, CFL 0.6, radius 0.2, "
+                        f"Sequential splitting, {cycles} cycles",
             "nx": nx, "ny": ny, "nghost": 5, "gamma": 1.4, "scheme": "GAD", "limiter": "Minmod",
-            "projection": "euler_2nd", "splitting": "Sequential", "cfl": 0.6, "radius": 0.2,
+            "projection": "euler_2nd", "splitting": "Sequential", "cfl": 0.6, "radius": 0.2, "run_cycles": cycles,
             "step": "one solver cycle (dt_CFL + X pass + Y pass)",
             "l2": "inputs larger than L2 (state: 4 arrays x %d MB per buffer set)" % ((nx + 10) * (ny + 10) * esize // 2**20),
             "parallelism": f"replicas x{n}" if n > 1 else "single domain"}
@@ -67,12 +78,6 @@ def profiled(key: str, precision: int = 64) -> float | None:
     return float(m.group(1)) if m else None
 
 
-def profiled_traffic(precision: int = 64, prefix: str = "") -> float | None:
-    """DRAM bytes per cell and axis pass (scaled to the workload by the caller); prefix "fused_" /
-    "split_" selects the figure of the pass form that is not the precision's default."""
-    return profiled(prefix + "traffic_bytes_per_cell_per_pass", precision)
-
-
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -91,6 +96,7 @@ class ClockSampler:
             self.t.start()
         except Exception:
             self.proc = None
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -104,74 +110,36 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = []
-        for ln in self.lines:
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) >= 9:
-                try:
-                    rows.append(parts)
-                except Exception:
-                    pass
+        rows = [[x.strip() for x in ln.split(",")] for ln in self.lines]
+        rows = [r for r in rows if len(r) >= 9]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         # the busiest GPU (highest power) is ours
         by_gpu: dict[str, list] = {}
         for r in rows:
             by_gpu.setdefault(r[0], []).append(r)
-        gpu = max(by_gpu, key=lambda g: statistics.median(float(r[3]) for r in by_gpu[g] if r[3] not in ("", "[N/A]")))
+
+        def med_power(g):
+            ps = [float(r[3]) for r in by_gpu[g] if r[3] not in ("", "[N/A]")]
+            return statistics.median(ps) if ps else 0.0
+
+        gpu = max(by_gpu, key=med_power)
         rs = by_gpu[gpu]
-        sm = [float(r[1]) for r in rs]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rs for k in range(4) if r[5 + k].lower() == "active"})
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rs[0][2]), "reasons": reasons,
-                "samples": len(rs), "power_w_median": statistics.median(float(r[3]) for r in rs)}
+        return {"sm_mhz": statistics.median(float(r[1]) for r in rs), "sm_max_mhz": float(rs[0][2]),
+                "reasons": reasons, "samples": len(rs), "power_w_median": med_power(gpu)}
 
 
-def fp64_roofline(cells: int, s_per_cycle: float, clocks: dict | None, prefix: str = "") -> dict | None:
-    """The FP64 pipe as the bound: FP64 operations per cell and axis pass (ncu's DADD + DMUL + DFMA
-    counts, profiles/) over the pipe's peak, 2 per SM per cycle (ncu's peak_sustained) at the SM
-    clock sampled during the timed region."""
-    import torch
-
-    ops = profiled(prefix + "fp64_ops_per_cell_per_pass")
-    if not ops:
-        return None
-    sms = torch.cuda.get_device_properties(0).multi_processor_count
-    mhz = (clocks or {}).get("sm_mhz") or 2070.0
-    peak = 2.0 * sms * mhz * 1e6
-    achieved = ops * cells * 2 / s_per_cycle
-    return {"bound": "fp64", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G FP64 op/s",
-            "frac": achieved / peak, "ops_per_cell_per_pass": ops,
-            "note": "divisions, square roots and compares run on the integer pipes (exact), so only "
-                    "additions and multiplications count here"}
-
-
-def l1_rel(a, b) -> float:
-    """sum |a - b| / sum |b| (b the FP64 result)."""
-    import numpy as np
-
-    return float(np.abs(a - b).sum() / np.abs(b).sum())
-
-
-def fp32_accuracy(A, case, graph: int) -> dict:
-    """The FP32 variant against the FP64 solve of the same case and cycles (the FP64 solver is
-    bit-identical to the FP64 oracle): L1 relative error of rho and E, and the relative drift of the
-    mass and energy sums (FP64 sums in both) over the run."""
-    res = {}
-    for prec in (64, 32):
-        with A.Solver(case, precision=prec, cycles_per_graph=graph) as s:
-            s.init_test()
-            m0, e0 = s.conservation()
-            s.run()
-            p, status = s.state()
-            m1, e1 = s.conservation()
-            res[prec] = ({k: A.real_cells(s.params, s.download(k)) for k in ("rho", "Emat")},
-                         (m1 - m0) / m0, (e1 - e0) / e0, p.cycle, status)
-    f64, f32 = res[64], res[32]
-    return {"cycles": f32[3], "l1_rho": l1_rel(f32[0]["rho"], f64[0]["rho"]),
-            "l1_E": l1_rel(f32[0]["Emat"], f64[0]["Emat"]),
-            "mass_drift": {"f32": f32[1], "f64": f64[1]}, "energy_drift": {"f32": f32[2], "f64": f64[2]},
-            "against": "the FP64 solve of the same workload and cycles (bit-identical to the FP64 oracle)"}
+def sampled(fn):
+    """Runs fn() with the clock sampler on; returns (fn's result, clocks)."""
+    smp = ClockSampler().start()
+    time.sleep(0.2)
+    try:
+        out = fn()
+    finally:
+        clocks = smp.stop()
+    return out, clocks
 
 
 def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
@@ -193,43 +161,73 @@ def dist_info() -> tuple[int, int, int]:
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def cpu_port_throughput(nx: int, ny: int, budget_s: float, max_cycles: int) -> dict:
-    """The oracle's OpenMP build with the reference's Release flags, on the host cores."""
-    import oracle_lib as O
+def l1_rel(a, b) -> float:
+    """sum |a - b| / sum |b| (b the reference result)."""
+    import numpy as np
 
-    L = O.lib(fast=True)
-    case = O.Case(**{k: v for k, v in WORKLOAD.items()})
-    case.nx, case.ny = nx, ny
-    p = O.make_params(case, L)
-    st = O.OracleState(p)
-    L.o_init_test_p(C.byref(p), C.byref(st.data), 0)
-    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
-    L.o_update_axis(C.byref(p), 0)
-    L.o_update_EOS(C.byref(p), C.byref(st.data))
-    t0 = time.perf_counter()
-    n = 0
-    while n < max_cycles:
-        if L.o_solver_cycle(C.byref(p), C.byref(st.data)) != 0:
-            break
-        p.time += p.current_cycle_dt
-        p.cycle += 1
-        n += 1
-        if time.perf_counter() - t0 >= budget_s:
-            break
-    secs = time.perf_counter() - t0
-    return {"value": nx * ny * n / secs, "unit": METRIC, "cores": L.o_num_threads(), "kind": "port",
-            "sample": f"{n} cycles of the {nx}x{ny} workload after init (oracle/armon_oracle.c, -O3 -ffast-math, OpenMP)",
-            "seconds": secs, "cycles": n}
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
 
 
-def run_reference(args) -> None:
-    rank, world, _ = dist_info()
-    if rank != 0:
-        return
-    nx = ny = args.size
-    os.environ.setdefault("OMP_PROC_BIND", "close")
-    os.environ.setdefault("OMP_PLACES", "cores")
-    # W untimed cycles are included in the same run as warm-up of caches and page faults
+def max_rel(a, b) -> float:
+    """max |a - b| / |b| over the cells where b != 0, and max |a - b| where b == 0."""
+    import numpy as np
+
+    d = np.abs(a - b)
+    nz = b != 0
+    m1 = float((d[nz] / np.abs(b[nz])).max()) if nz.any() else 0.0
+    m0 = float(d[~nz].max()) if (~nz).any() else 0.0
+    return max(m1, m0)
+
+
+# ---------------------------------------------------------------- the reference's CPU path
+def reference_driver() -> str | None:
+    """oracle/_ref/fast/ref_driver: the reference's own sources (staged in baseline/_ref) with its
+    Release flags, built on this machine on first use; None when the tree is not there."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "fast", "ref_driver")
+    if not os.path.exists(exe):
+        if not os.path.isdir(os.path.join(ROOT, "baseline", "_ref", "src", "kernels")):
+            return None
+        r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref-fast", f"-j{os.cpu_count() or 4}"],
+                           capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(exe):
+            return None
+    return exe
+
+
+def cpu_model() -> str:
+    try:
+        m = re.search(r"Model name:\s*(.+)", subprocess.run(["lscpu"], capture_output=True, text=True).stdout)
+        return m.group(1).strip() if m else ""
+    except OSError:
+        return ""
+
+
+def reference_cpu(nx: int, ny: int, cycles: int, warmup: int) -> dict:
+    """The reference's time_loop (src/armon_2D.cpp:327-386) on the host cores: `warmup` cycles, then
+    `cycles` timed by the reference itself; the rate is its grind time's inverse
+    (src/armon_2D.cpp:374-382)."""
+    exe = reference_driver()
+    if exe is None:
+        raise RuntimeError("the reference tree is not staged (make -C oracle stage)")
+    threads = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="close", OMP_PLACES="cores")
+    args = [exe, "-", "test=Sod_circ", "scheme=GAD", "projection=euler_2nd", "limiter=Minmod",
+            "splitting=Sequential", "nghost=5", f"nx={nx}", f"ny={ny}", "cfl=0.6", "max_time=1e9",
+            "radius2=0.04", f"bench_cycles={cycles}", f"bench_warmup={warmup}"]
+    r = subprocess.run(args, capture_output=True, text=True, env=env, check=True)
+    kv = dict(tok.split("=") for tok in r.stdout.strip().splitlines()[-1].split()[1:])
+    grind_us = float(kv["grind_us"])
+    return {"value": 1e6 / grind_us, "unit": METRIC, "cores": int(kv["threads"]), "kind": "reference",
+            "sample": f"{kv['cycles']} cycles of the {nx}x{ny} workload after {warmup} warm-up cycles: the reference's "
+                      "own time_loop and grind time (its src/ and src/kernels/ compiled unchanged against the "
+                      "project's Kokkos API shim, -O3 -funroll-loops -ffast-math, OpenMP static schedule)",
+            "seconds": float(kv["seconds"]), "grind_us_per_cell_cycle": grind_us, "cpu": cpu_model(),
+            "omp": "OMP_PROC_BIND=close OMP_PLACES=cores"}
+
+
+def port_cpu(nx: int, ny: int, cycles: int) -> dict:
+    """The oracle (the project's C restatement of the reference) built with the reference's Release
+    flags, OpenMP on the host cores, `cycles` cycles after init."""
     import oracle_lib as O
 
     L = O.lib(fast=True)
@@ -241,33 +239,181 @@ def run_reference(args) -> None:
     p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
     L.o_update_axis(C.byref(p), 0)
     L.o_update_EOS(C.byref(p), C.byref(st.data))
-
-    def cycle():
+    t0 = time.perf_counter()
+    for _ in range(cycles):
         assert L.o_solver_cycle(C.byref(p), C.byref(st.data)) == 0
         p.time += p.current_cycle_dt
         p.cycle += 1
-
-    for _ in range(args.warmup):
-        cycle()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        cycle()
     secs = time.perf_counter() - t0
-    value = nx * ny * args.steps / secs
+    return {"value": nx * ny * cycles / secs, "unit": METRIC, "cores": L.o_num_threads(), "kind": "port",
+            "sample": f"{cycles} cycles of the {nx}x{ny} workload after init (oracle/armon_oracle.c, -O3 -ffast-math, "
+                      "OpenMP)", "seconds": secs}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    nx = ny = args.size
+    try:
+        cb = reference_cpu(nx, ny, args.steps, args.warmup)
+    except Exception as e:
+        cb = dict(port_cpu(nx, ny, args.steps), note=f"reference build unavailable here ({e}); the oracle port instead")
+    value = cb["value"]
     out = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": nx * ny / value * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": config(nx, ny, 1),
-           "cpu_baseline": {"value": value, "unit": METRIC, "cores": L.o_num_threads(), "kind": "port",
-                            "sample": f"{args.steps} timed cycles of the {nx}x{ny} workload on the host cores "
-                                      "(oracle/armon_oracle.c: the reference's unfused stage sequence, OpenMP, "
-                                      "-O3 -funroll-loops -ffast-math)"},
+           "config": config(nx, ny, 1), "cpu_baseline": cb,
            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
-def run_gpu(args) -> None:
+# ---------------------------------------------------------------- parity against the oracle
+def parity(A, case, cycles: int, precision: int = 64) -> dict:
+    """The GPU solver (default options: measured tiling, longest-first dispatch, split passes, reuse)
+    against the strict oracle, cycle by cycle: max and L1 relative error per field after `cycles`
+    cycles, and the largest relative difference of (current dt, next dt, time) over every cycle."""
     import numpy as np
+
+    import oracle_lib as O
+
+    L = O.lib()
+    c = O.Case(**{**case.__dict__, "max_cycles": cycles})
+    p = O.make_params(c, L)
+    st = O.OracleState(p)
+    L.o_init_test_p(C.byref(p), C.byref(st.data), 0)
+    p.cycle, p.time, p.current_cycle_dt, p.next_cycle_dt = 0, 0.0, 0.0, 0.0
+    L.o_update_axis(C.byref(p), 0)
+    L.o_update_EOS(C.byref(p), C.byref(st.data))
+    t0 = time.perf_counter()
+    ref_steps = []
+    for _ in range(cycles):
+        assert L.o_solver_cycle(C.byref(p), C.byref(st.data)) == 0
+        p.time += p.current_cycle_dt
+        p.cycle += 1
+        ref_steps.append((p.current_cycle_dt, p.next_cycle_dt, p.time))
+    oracle_s = time.perf_counter() - t0
+    ref = {k: O.real_cells(p, st[k]).copy() for k in PARITY_FIELDS}
+    del st
+    gcase = A.Case(**{**case.__dict__, "max_cycles": cycles})
+    steps = []
+    with A.Solver(gcase, precision=precision) as s:
+        s.init_test()
+        for _ in range(cycles):
+            s.enqueue_cycles(1)
+            q, status = s.state()
+            assert status == 0
+            steps.append((q.current_cycle_dt, q.next_cycle_dt, q.time))
+        s.run()
+        got = {k: A.real_cells(s.params, s.download(k)) for k in PARITY_FIELDS}
+    dt_err = max(abs(a - b) / abs(b) for sa, sb in zip(steps, ref_steps) for a, b in zip(sa, sb))
+    fields = {k: {"max_rel": max_rel(got[k], ref[k]), "l1_rel": l1_rel(got[k], ref[k]),
+                  "bitwise_equal": bool(np.array_equal(got[k].view(np.int64), ref[k].view(np.int64)))}
+              for k in PARITY_FIELDS}
+    return {"cycles": cycles, "size": f"{case.nx}x{case.ny}", "fields": fields, "dt_time_max_rel": dt_err,
+            "cycles_equal": len(steps) == len(ref_steps),
+            "against": "the oracle (strict IEEE build of the project's C restatement, pinned bit for bit to the "
+                       "reference's own code by tests/golden), cycle by cycle; tolerance 1e-10 relative on fields, "
+                       "1e-12 on dt (the tests assert bit equality)",
+            "oracle_seconds": oracle_s}
+
+
+# ---------------------------------------------------------------- the single-domain path
+def single_run(A, args, nx: int, prec: int, K: int, W: int, run_cycles: int, stream, world: int) -> dict:
+    """One domain: the timed K cycles are the last of a `run_cycles` run (at least 80 cycles precede
+    the W warm-up cycles; the first of them measure the tiling when this process has not).  Returns
+    the timings and the solver."""
+    import torch
+
+    total = max(run_cycles, W + K + 80)
+    case = A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": total})
+    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len,
+                 block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
+    s.init_test()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    s.enqueue_cycles(total - W - K)
+    s.enqueue_cycles(W)
+    torch.cuda.synchronize()
+    tuning_left = s.tuning()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = s.kernel_launches
+
+    def timed():
+        ev[1].record(stream)
+        s.enqueue_cycles(K)
+        ev[2].record(stream)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        return ev[1].elapsed_time(ev[2])
+
+    ms, clocks = sampled(timed)
+    launches = s.kernel_launches - launches0
+    p, status = s.state()
+    if status != 0 or p.cycle != total:
+        raise RuntimeError(f"solver state after the timed region: status {status}, cycle {p.cycle}")
+    tiling, blocks = s.tiling()
+    return {"ms": ms, "whole_ms": ev[0].elapsed_time(ev[2]), "total": total, "clocks": clocks, "launches": launches,
+            "tiling": tiling, "blocks": blocks, "block_lines": s.block_lines(), "tuning_left": tuning_left,
+            "split": s.split_pass(), "solver": s}
+
+
+def e2e_run(A, args, nx: int, prec: int, cycles: int, stream, ins: dict, cold: bool) -> tuple[float, int]:
+    """The whole solve through the C ABI with host buffers: upload of rho, u, v, E from pinned
+    memory, begin_loop, `cycles` cycles, download of rho, u, v, E, p (wall clock).  cold: the
+    process forgets its measured tilings first, so the solve measures its own."""
+    import torch
+
+    case = A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": cycles})
+    se = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
+                  seg_len=args.seg_len, block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
+    se.init_test()
+    outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
+            for k in ("rho", "umat", "vmat", "Emat", "pmat")}
+    L = A.lib()
+    if cold:
+        A.tiling_cache_clear()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for name in ("rho", "umat", "vmat", "Emat"):
+        A.check(L.armon_solver_upload(se._h, A.ARRAYS.index(name), ins[name].data_ptr()))
+    se.begin_loop()
+    se.run()
+    for name in ("rho", "umat", "vmat", "Emat", "pmat"):
+        A.check(L.armon_solver_download(se._h, A.ARRAYS.index(name), outs[name].data_ptr()))
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    pe, st_e = se.state()
+    assert st_e == 0 and pe.cycle == cycles
+    nb = se.params.nb_cells
+    se.close()
+    return secs, nb
+
+
+def roofline(prec: int, cells: int, ms_per_cycle: float, split: bool) -> dict:
+    peak, peak_kind = measured_peaks()
+    t_pass = ms_per_cycle / 1e3 / 2
+    bpc = BYTES_PER_CELL_UPDATE if prec == 64 else BYTES_PER_CELL_UPDATE // 2
+    achieved = bpc / 2 * cells / t_pass / 1e9
+    tname = "double" if prec == 64 else "float"
+    kernel = ("armon::sweep_faces_kernel<%s,1,2,*> + armon::sweep_cells_kernel<%s,1,2,*> (one axis pass = a face "
+              "launch and a cell launch)" % (tname, tname) if split else
+              "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)" % tname)
+    key = ("split_" if split else "fused_") + "traffic_bytes_per_cell_per_pass"
+    tr = profiled(key, prec)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, a STREAM-style copy)",
+            "traffic": (tr * cells if tr else None), "traffic_bytes_per_cell_per_pass": tr,
+            "kernel": kernel, "algorithmic_bytes_per_pass": bpc / 2 * cells,
+            "per_unit": f"{bpc // 2} B per cell and axis pass (read and write rho, u, v, E once per cycle: "
+                        f"{bpc} B per cell-update), over the mean axis-pass time of the timed cycles"}
+
+
+def run_gpu(args) -> None:
     import torch
 
     import armon_gb300 as A
@@ -277,127 +423,114 @@ def run_gpu(args) -> None:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    nx = ny = args.size
-    K, W = args.steps, args.warmup
-    case = A.Case(**WORKLOAD)
-    case.nx, case.ny = nx, ny
-    case.max_cycles = W + K
-    prec = args.precision
+    nx = args.size
+    K, W, prec = args.steps, args.warmup, args.precision
+    run_cycles = args.run_cycles or (200 if prec == 64 else 100)
     # a dedicated stream: the solver launches on it and the CUDA events are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    s = A.Solver(case, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph, seg_len=args.seg_len,
-                 block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
-    s.init_test()
-    s.enqueue_cycles(W)
-    torch.cuda.synchronize()
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    barrier()
-    launches0 = s.kernel_launches
-    tiling = s.tiling()
-    block_lines = s.block_lines()
-    sampler = ClockSampler() if rank == 0 else None
-    if sampler:
-        sampler.start()
-        time.sleep(0.25)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    s.enqueue_cycles(K)
-    e1.record(stream)
-    barrier()
-    clocks = sampler.stop() if sampler else None
-    ms = e0.elapsed_time(e1)
-    launches = s.kernel_launches - launches0
-    p, status = s.state()
-    if status != 0 or p.cycle != W + K:
-        raise RuntimeError(f"solver state after the timed region: status {status}, cycle {p.cycle}")
-    ms_max = max_over_ranks(ms, world)
-    cells = nx * ny
+    r = single_run(A, args, nx, prec, K, W, run_cycles, stream, world)
+    r.pop("solver").close()
+    cells = nx * nx
+    ms_max = max_over_ranks(r["ms"], world)
     value = whole_job_rate(cells * K, world, ms_max / 1e3)
-
-    # end to end through the C ABI with host buffers: H2D of the initial fields from pinned memory,
-    # the time loop, D2H of rho, u, v, E, p (every step of it inside the timed region)
-    ins = {k: torch.from_numpy(s.download(k)).pin_memory() for k in ("rho", "umat", "vmat", "Emat")}
-    s.close()
-    case_e2e = A.Case(**WORKLOAD)
-    case_e2e.nx, case_e2e.ny = nx, ny
-    case_e2e.max_cycles = K
-    se = A.Solver(case_e2e, precision=prec, stream=stream.cuda_stream, cycles_per_graph=args.graph,
-                  seg_len=args.seg_len, block_lines=args.block_lines, split_pass=args.split_pass, reuse=args.reuse)
-    se.init_test()
-    outs = {k: torch.empty(se.params.nb_cells, dtype=torch.float64).pin_memory()
-            for k in ("rho", "umat", "vmat", "Emat", "pmat")}
-    L = A.lib()
-    barrier()
-    t0 = time.perf_counter()
-    for k, name in enumerate(("rho", "umat", "vmat", "Emat")):
-        A.check(L.armon_solver_upload(se._h, A.ARRAYS.index(name), ins[name].data_ptr()))
-    se.begin_loop()
-    se.run()
-    for name in ("rho", "umat", "vmat", "Emat", "pmat"):
-        A.check(L.armon_solver_download(se._h, A.ARRAYS.index(name), outs[name].data_ptr()))
-    barrier()
-    e2e_s = time.perf_counter() - t0
-    pe, st_e = se.state()
-    assert st_e == 0 and pe.cycle == K
-    se.close()
-    nb = se.params.nb_cells if hasattr(se, "params") else (nx + 10) * (ny + 10)
-    e2e_value = whole_job_rate(cells * K, world, max_over_ranks(e2e_s, world))
+    whole = whole_job_rate(cells * r["total"], world, max_over_ranks(r["whole_ms"], world) / 1e3)
+    # end to end, from the run's initial state (init_test of a fresh solver) in pinned host memory
+    with A.Solver(A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": 1}), precision=prec) as s0:
+        s0.init_test()
+        ins = {k: torch.from_numpy(s0.download(k)).pin_memory() for k in ("rho", "umat", "vmat", "Emat")}
+    e2e_s, nb = e2e_run(A, args, nx, prec, run_cycles, stream, ins, cold=False)
+    e2e_value = whole_job_rate(cells * run_cycles, world, max_over_ranks(e2e_s, world))
+    cold_s, _ = e2e_run(A, args, nx, prec, run_cycles, stream, ins, cold=True)
+    cold_value = whole_job_rate(cells * run_cycles, world, max_over_ranks(cold_s, world))
 
     if rank == 0:
-        peak, peak_kind = measured_peaks()
-        t_launch = ms_max / 1e3 / (K * 2)
-        bpc = BYTES_PER_CELL_UPDATE if prec == 64 else BYTES_PER_CELL_UPDATE // 2
-        achieved = bpc / 2 * cells / t_launch / 1e9
-        split = args.split_pass == 1 or (args.split_pass == 0 and prec == 64)
-        prefix = "" if split == (prec == 64) else ("fused_" if prec == 64 else "split_")
-        tr = profiled_traffic(prec, prefix)
-        tname = "double" if prec == 64 else "float"
-        kernel = ("armon::sweep_faces_kernel<%s,1,*> + armon::sweep_cells_kernel<%s,1,2,*> (one axis pass = a face "
-                  "launch and a cell launch)" % (tname, tname) if split else
-                  "armon::sweep_kernel<%s,1,2,*> (one launch = one axis pass)" % tname)
         out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64" if prec == 64 else "f32", "data": "synthetic",
-               "config": dict(config(nx, ny, world, prec), seg_len=list(tiling[0]), blocks=list(tiling[1]),
-                             block_lines=block_lines),
-               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "peak_source": peak_kind,
-                            "traffic": (tr * cells if tr else None),
-                            "kernel": kernel,
-                            "algorithmic_bytes_per_pass": bpc / 2 * cells,
-                            "note": ("not HBM-bound: the FP64 pipe and integer latency bound the pass (fp64_roofline, profiles/)"
-                                     if prec == 64 else
-                                     "not HBM-bound: instruction latency bounds the pass (12 warps per SM; profiles/)")},
-               "fp64_roofline": fp64_roofline(cells, ms_max / 1e3 / K, clocks, prefix) if prec == 64 else None,
-               "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * nb * 8 / K,
-                       "d2h_bytes_per_step": 5 * nb * 8 / K, "seconds": e2e_s,
-                       "host_arrays": "FP64 (converted to the solver's precision inside the call)",
-                       "path": "armon_solver_upload x4 (pinned) + begin_loop + run + armon_solver_download x5"},
-               "gpu_launches": launches, "clocks": clocks}
+               "config": dict(config(nx, nx, world, prec, r["total"]), seg_len=list(r["tiling"]),
+                              blocks=list(r["blocks"]), block_lines=r["block_lines"], split_pass=r["split"],
+                              reuse=args.reuse == 0, timed_cycles=[r["total"] - K, r["total"]],
+                              tiling_measured_before_timing=not r["tuning_left"]),
+               "whole_run": {"value": whole, "unit": METRIC, "cycles": r["total"],
+                             "note": "every cycle of the run on the device (CUDA events), the tiling measurement's "
+                                     "cycles included"},
+               "roofline": roofline(prec, cells, ms_max / K, r["split"]),
+               "e2e": {"value": e2e_value, "unit": METRIC, "cycles": run_cycles,
+                       "h2d_bytes_per_step": 4 * nb * 8 / run_cycles, "d2h_bytes_per_step": 5 * nb * 8 / run_cycles,
+                       "seconds": e2e_s, "host_arrays": "FP64 (converted to the solver's precision inside the call)",
+                       "path": f"armon_solver_upload x4 (pinned) + begin_loop + {run_cycles} cycles + "
+                               "armon_solver_download x5; tiling already measured in this process"},
+               "e2e_cold": {"value": cold_value, "unit": METRIC, "seconds": cold_s, "cycles": run_cycles,
+                            "path": "the same after armon_tiling_cache_clear(): the solve measures its tiling on "
+                                    "its own cycles"},
+               "gpu_launches": r["launches"], "clocks": r["clocks"]}
+        if world == 1 and args.parity_cycles > 0 and prec == 64:
+            out["parity"] = parity(A, A.Case(**{**WORKLOAD, "nx": nx, "ny": nx}), min(args.parity_cycles, run_cycles))
         if world == 1 and not args.no_cpu and prec == 64:
-            out["cpu_baseline"] = cpu_port_throughput(nx, ny, args.cpu_seconds, 200)
+            try:
+                out["cpu_baseline"] = reference_cpu(nx, nx, args.cpu_cycles, 1)
+            except Exception as e:
+                out["cpu_baseline"] = dict(port_cpu(nx, nx, args.cpu_cycles), note=f"reference build unavailable ({e})")
+            out["cpu_baseline_port"] = port_cpu(nx, nx, args.cpu_cycles)
         if world == 1 and prec == 32 and args.accuracy_cycles > 0:
-            acc_case = A.Case(**WORKLOAD)
-            acc_case.nx, acc_case.ny = nx, ny
-            acc_case.max_cycles = args.accuracy_cycles
-            out["accuracy"] = fp32_accuracy(A, acc_case, args.graph)
+            out["accuracy"] = fp32_accuracy(A, nx, args.accuracy_cycles, args.graph)
+        if world == 1 and prec == 64 and not args.no_extra:
+            out["fp32"] = fp32_line(A, args, stream)
+            out["batch"] = batch_line(args, compact=True)
+            out["serve"] = serve_line(args, compact=True)
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def plain_solve(A, spec, precision: int, graph: int, block_lines: int = 0) -> tuple[float, int]:
+# ---------------------------------------------------------------- configuration 5: the FP32 variant
+def fp32_accuracy(A, nx: int, cycles: int, graph: int) -> dict:
+    """The FP32 variant against the FP64 solve of the same workload and cycles (the FP64 solver
+    equals the oracle bit for bit: tests/test_scale_parity_gpu.py): L1 relative error of rho and E,
+    and the relative drift of the FP64 mass and energy sums over the run."""
+    res = {}
+    for prec in (64, 32):
+        case = A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": cycles})
+        with A.Solver(case, precision=prec, cycles_per_graph=graph) as s:
+            s.init_test()
+            m0, e0 = s.conservation()
+            s.run()
+            p, status = s.state()
+            m1, e1 = s.conservation()
+            res[prec] = ({k: A.real_cells(s.params, s.download(k)) for k in ("rho", "Emat")},
+                         (m1 - m0) / m0, (e1 - e0) / e0, p.cycle, status)
+    f64, f32 = res[64], res[32]
+    return {"cycles": f32[3], "l1_rho": l1_rel(f32[0]["rho"], f64[0]["rho"]),
+            "l1_E": l1_rel(f32[0]["Emat"], f64[0]["Emat"]),
+            "mass_drift": {"f32": f32[1], "f64": f64[1]}, "energy_drift": {"f32": f32[2], "f64": f64[2]},
+            "against": "the FP64 solve of the same workload and cycles (equal to the FP64 oracle bit for bit)"}
+
+
+def fp32_line(A, args, stream) -> dict:
+    """Configuration 5 compact: 8192^2 FP32, the last K cycles of a 100-cycle run timed, and the
+    accuracy of the 100-cycle run against FP64."""
+    nx, K, W = 8192, args.steps, args.warmup
+    r = single_run(A, argparse.Namespace(**{**vars(args), "split_pass": 0}), nx, 32, K, W, 100, stream, 1)
+    r.pop("solver").close()
+    cells = nx * nx
+    return {"value": cells * K / (r["ms"] / 1e3), "unit": METRIC, "ms_per_step": r["ms"] / K, "steps": K, "warmup": W,
+            "config": dict(config(nx, nx, 1, 32, r["total"]), seg_len=list(r["tiling"]), block_lines=r["block_lines"],
+                           split_pass=r["split"], timed_cycles=[r["total"] - K, r["total"]]),
+            "whole_run": {"value": cells * r["total"] / (r["whole_ms"] / 1e3), "cycles": r["total"]},
+            "roofline": roofline(32, cells, r["ms"] / K, r["split"]),
+            "accuracy": fp32_accuracy(A, nx, 100, args.graph) if args.accuracy_cycles > 0 else None,
+            "gpu_launches": r["launches"], "clocks": r["clocks"]}
+
+
+# ---------------------------------------------------------------- configuration 3: batches
+def plain_solve(A, spec, precision: int, graph: int, block_lines: int = 0, reuse: int = 0) -> tuple[float, int]:
     """One domain on the plain single-domain path (its own solver: init, upload of the initial
     fields, time loop); returns the seconds of its time loop and its cell-updates."""
     import torch
 
-    with A.Solver(spec.params(), precision=precision, cycles_per_graph=graph, block_lines=block_lines) as s:
+    with A.Solver(spec.params(), precision=precision, cycles_per_graph=graph, block_lines=block_lines,
+                  reuse=reuse) as s:
         s.init_test()
         for k, a in spec.initial_state().items():
             s.upload(k, a)
@@ -411,10 +544,19 @@ def plain_solve(A, spec, precision: int, graph: int, block_lines: int = 0) -> tu
         return secs, spec.nx * spec.ny * p.cycle
 
 
-def run_batch(args) -> None:
-    """Configuration 3: 256 uneven domains (seeded), FP64, each to t = 0.15 -- all of them in one
-    batch (one fused launch per pass, CUDA graphs) against the same domains one after another on the
-    plain single-domain path."""
+def stratified(items: list, key, n: int) -> list:
+    """n items spread evenly over the list sorted by key (one from each of n equal slices)."""
+    if n >= len(items):
+        return list(items)
+    srt = sorted(items, key=key)
+    step = len(srt) / n
+    return [srt[int(i * step + step / 2)] for i in range(n)]
+
+
+def batch_line(args, compact: bool) -> dict:
+    """Configuration 3: 256 uneven domains (seeded), FP64, each to t = 0.15, all in one batch (one
+    launch per pass half over every domain, CUDA graphs), against the plain single-domain path (one
+    solver per domain, one after another) on the same domains, or on a stratified sample of them."""
     import torch
 
     import armon_gb300 as A
@@ -422,24 +564,24 @@ def run_batch(args) -> None:
 
     specs = W.mixed_domains(args.domains, seed=2024)
     torch.cuda.set_device(0)
-    # plain path (domains one at a time; the first is a warm-up)
+    sample = stratified(specs, lambda sp: sp.nx * sp.ny, args.plain_domains) if compact else specs
+    plain_solve(A, sample[0], 64, args.graph, args.block_lines, args.reuse)   # warm-up
     plain_secs, plain_work = 0.0, 0
-    plain_solve(A, specs[0], 64, args.graph, args.block_lines)
-    for sp in specs:
-        s_, w_ = plain_solve(A, sp, 64, args.graph, args.block_lines)
+    for sp in sample:
+        s_, w_ = plain_solve(A, sp, 64, args.graph, args.block_lines, args.reuse)
         plain_secs += s_
         plain_work += w_
-    # batched
-    with A.Batch(precision=64, cycles_per_graph=8, block_lines=args.block_lines or 128) as b:
+    with A.Batch(precision=64, cycles_per_graph=8, block_lines=args.block_lines or 128, reuse=args.reuse) as b:
         ids = [b.add_sod(sp.params(), sp.sod_interface()) for sp in specs]
         b.poll()
         launches0 = b.kernel_launches
-        sampler = ClockSampler()
-        sampler.start()
-        t0 = time.perf_counter()
-        assert b.run() == 0
-        secs = time.perf_counter() - t0
-        clocks = sampler.stop()
+
+        def go():
+            t0 = time.perf_counter()
+            assert b.run() == 0
+            return time.perf_counter() - t0
+
+        secs, clocks = sampled(go)
         launches = b.kernel_launches - launches0
         waves, _ = b.schedule()
         work = 0
@@ -447,45 +589,43 @@ def run_batch(args) -> None:
             p, st = b.state(i)
             assert st == 0
             work += sp.nx * sp.ny * p.cycle
-    assert work == plain_work
     value = work / secs
-    cells = sum(sp.nx * sp.ny for sp in specs)
-    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 1, "warmup": 1,
-           "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"{len(specs)} uneven Sod-interface domains (seed 2024), sides in "
-                                  "{64..1024}, GAD-minmod + euler_2nd, CFL 0.6, each to t = 0.15",
-                      "domains": len(specs), "cells": cells, "cell_updates": work,
-                      "step": "the whole batch run to completion (one fused launch per pass, 8-cycle CUDA graphs)"},
-           "plain": {"value": plain_work / plain_secs, "seconds": plain_secs,
-                     "path": "one Solver per domain, one after another (time loops only)"},
-           "batched_over_plain": value / (plain_work / plain_secs),
-           "schedule": {"waves": waves, "how": "autotuned online (CUDA-event timing of one graph batch per candidate)"},
-           "gpu_launches": launches, "clocks": clocks}
-    print(json.dumps(out), flush=True)
+    plain_value = plain_work / plain_secs
+    return {"metric": METRIC, "value": value, "unit": METRIC, "seconds": secs, "dtype": "f64",
+            "config": {"workload": f"{len(specs)} uneven Sod-interface domains (seed 2024), sides in {{64..1024}}, "
+                                   "GAD-minmod + euler_2nd, CFL 0.6, each to t = 0.15",
+                       "domains": len(specs), "cells": sum(sp.nx * sp.ny for sp in specs), "cell_updates": work,
+                       "step": "the whole batch run to completion (one launch per pass half over every domain, "
+                               "8-cycle CUDA graphs)"},
+            "plain": {"value": plain_value, "seconds": plain_secs, "domains": len(sample),
+                      "sample": ("a stratified sample by domain size (one domain from each of %d equal slices of the "
+                                 "%d sorted by cells)" % (len(sample), len(specs))) if len(sample) < len(specs) else "all",
+                      "path": "one Solver per domain, one after another (time loops only)"},
+            "batched_over_plain": value / plain_value,
+            "schedule": {"waves": waves, "how": "autotuned online (CUDA-event timing of one graph batch per candidate)"},
+            "gpu_launches": launches, "clocks": clocks}
 
 
-def run_serve(args) -> None:
+# ---------------------------------------------------------------- configuration 4: serving
+def serve_line(args, compact: bool) -> dict:
     """Configuration 4: Poisson arrivals of Sod-interface solves (side lognormal(6, 0.6) clipped to
     [128, 2048], FP64 or FP32 with p = 1/2, t_end ~ U(0.05, 0.2)) replayed in real time through the
-    server with a 150 GB state budget; p50/p99 time-to-solution and cell-updates/s."""
+    server with a 150 GB state budget; p50/p99 time-to-solution and cell-updates/s, against the plain
+    path on a stratified sample of the same requests."""
     import torch
 
     import armon_gb300 as A
     from armon_gb300 import serving as S
     from armon_gb300 import workloads as W
 
-    trace = W.serving_trace(n=args.requests, rate=args.rate, seed=7)
+    n = args.serve_requests_compact if compact else args.requests
+    trace = W.serving_trace(n=n, rate=args.rate, seed=7)
     torch.cuda.set_device(0)
-    # warm-up: the kernels of both precisions
-    with A.Server(cycles_per_step=args.serve_cycles) as srv:
+    with A.Server(cycles_per_step=args.serve_cycles) as srv:      # warm-up: the kernels of both precisions
         S.replay(srv, W.serving_trace(n=4, rate=1000.0, seed=1, side_range=(128, 128)))
     with A.Server(memory_budget=150_000_000_000, cycles_per_step=args.serve_cycles,
                   max_inflight_cells=args.max_inflight, waves=args.serve_waves) as srv:
-        sampler = ClockSampler()
-        sampler.start()
-        served, wall = S.replay(srv, trace)
-        clocks = sampler.stop()
+        (served, wall), clocks = sampled(lambda: S.replay(srv, trace))
         launches = srv.kernel_launches
     assert all(r.status == A.REQ_DONE for r in served)
     work = sum(r.cells * r.cycles for r in served)
@@ -494,43 +634,39 @@ def run_serve(args) -> None:
     for prec in (64, 32):
         t = [r.tts for r in served if r.precision == prec]
         by_prec[str(prec)] = {"requests": len(t), "tts_p50_s": S.percentile(t, 0.5), "tts_p99_s": S.percentile(t, 0.99)}
-    # the plain path on a sample of the same requests, one solve at a time
-    sample = trace[:args.plain_sample]
+    sample = stratified(trace, lambda r: r.spec.nx * r.spec.ny, min(args.plain_sample, len(trace)))
     p_secs, p_work = 0.0, 0
     for r in sample:
-        s_, w_ = plain_solve(A, r.spec, r.spec.precision, args.graph)
+        s_, w_ = plain_solve(A, r.spec, r.spec.precision, args.graph, reuse=args.reuse)
         p_secs += s_
         p_work += w_
-    # FP32 requests against the same solve in FP64 (served results equal solo ones bit for bit)
-    l1 = []
-    for r in [r for r in trace if r.spec.precision == 32][:args.accuracy_sample]:
-        fields = {}
-        for prec in (64, 32):
-            with A.Solver(r.spec.params(), precision=prec) as s:
-                s.init_test()
-                for k, a in r.spec.initial_state().items():
-                    s.upload(k, a)
-                s.begin_loop()
-                s.run()
-                fields[prec] = {k: A.real_cells(s.params, s.download(k)) for k in ("rho", "Emat")}
-        l1.append((l1_rel(fields[32]["rho"], fields[64]["rho"]), l1_rel(fields[32]["Emat"], fields[64]["Emat"])))
     value = work / wall
-    out = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 1, "warmup": 1,
-           "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64+f32", "data": "synthetic",
-           "fp32_accuracy": {"requests": len(l1), "l1_rho_max": max((a for a, _ in l1), default=None),
-                             "l1_E_max": max((b for _, b in l1), default=None),
-                             "against": "each request solved alone in FP64 (to its own t_end; cycle counts may differ)"},
-           "config": {"workload": f"{len(trace)} requests, Poisson arrivals at {args.rate}/s (seed 7), side "
-                                  "lognormal(6, 0.6) clipped to [128, 2048], FP64 or FP32 (p = 1/2), t_end ~ U(0.05, 0.2), "
-                                  "150 GB state budget",
-                      "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work,
-                      "max_inflight_cells": args.max_inflight},
-           "tts_p50_s": S.percentile(tts, 0.5), "tts_p99_s": S.percentile(tts, 0.99), "by_precision": by_prec,
-           "plain": ({"value": p_work / p_secs, "seconds": p_secs, "sample": f"the first {len(sample)} requests",
-                      "path": "one Solver per request, one after another (time loops only)"} if sample else None),
-           "served_over_plain": value / (p_work / p_secs) if sample else None,
-           "gpu_launches": launches, "clocks": clocks}
+    return {"metric": METRIC, "value": value, "unit": METRIC, "seconds": wall, "dtype": "f64+f32",
+            "config": {"workload": f"{len(trace)} requests, Poisson arrivals at {args.rate}/s (seed 7), side "
+                                   "lognormal(6, 0.6) clipped to [128, 2048], FP64 or FP32 (p = 1/2), "
+                                   "t_end ~ U(0.05, 0.2), 150 GB state budget",
+                       "requests": len(trace), "cycles_per_round": args.serve_cycles, "cell_updates": work,
+                       "max_inflight_cells": args.max_inflight},
+            "tts_p50_s": S.percentile(tts, 0.5), "tts_p99_s": S.percentile(tts, 0.99), "by_precision": by_prec,
+            "plain": {"value": p_work / p_secs, "seconds": p_secs, "requests": len(sample),
+                      "sample": "a stratified sample of the same requests by size (one from each of n equal slices "
+                                "sorted by cells)",
+                      "path": "one Solver per request, one after another (time loops only)"},
+            "served_over_plain": value / (p_work / p_secs),
+            "gpu_launches": launches, "clocks": clocks}
+
+
+def run_batch(args) -> None:
+    out = batch_line(args, compact=False)
+    out.update({"n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": out["seconds"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
+    print(json.dumps(out), flush=True)
+
+
+def run_serve(args) -> None:
+    out = serve_line(args, compact=False)
+    out.update({"n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": out["seconds"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
     print(json.dumps(out), flush=True)
 
 
@@ -542,31 +678,35 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=0, help="cells per side (default 4096; 8192 for --precision 32)")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--run-cycles", type=int, default=0,
+                    help="cycles of the run whose last --steps cycles are timed (default 200; 100 for --precision 32)")
     ap.add_argument("--graph", type=int, default=16, help="cycles per CUDA graph")
     ap.add_argument("--seg-len", type=int, default=0, help="cells per thread along the sweep axis (0 = automatic)")
     ap.add_argument("--block-lines", type=int, default=0, help="threads (lines) per block of the axis pass (0 = automatic)")
     ap.add_argument("--split-pass", type=int, default=0, choices=[-1, 0, 1],
                     help="1: each axis pass as a face launch and a cell launch; -1: one fused launch; "
-                         "0: the solver's default (split in FP64)")
+                         "0: the solver's default (measured)")
     ap.add_argument("--reuse", type=int, default=0, choices=[-1, 0],
                     help="0: positions whose input window repeats the previous one reuse its results (exact); "
                          "-1: every position computed")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--parity-cycles", type=int, default=200, help="cycles compared with the oracle (0 = skip)")
+    ap.add_argument("--cpu-cycles", type=int, default=10, help="cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--accuracy-cycles", type=int, default=100,
-                    help="--precision 32: cycles of the FP32-vs-FP64 accuracy run (0 = skip)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the compact fp32 / batch / serve runs")
+    ap.add_argument("--accuracy-cycles", type=int, default=100, help="FP32 accuracy run's cycles (0 = skip)")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
                     help="single: the 4096^2 drop-in case (default); batch: 256 mixed domains; serve: a request trace")
-    ap.add_argument("--domains", type=int, default=256, help="--workload batch: domains")
-    ap.add_argument("--requests", type=int, default=2000, help="--workload serve: requests of the trace")
-    ap.add_argument("--rate", type=float, default=50.0, help="--workload serve: arrivals per second")
-    ap.add_argument("--serve-cycles", type=int, default=8, help="--workload serve: cycles per round")
+    ap.add_argument("--domains", type=int, default=256, help="batch: domains")
+    ap.add_argument("--plain-domains", type=int, default=32, help="batch in the default line: domains timed on the plain path")
+    ap.add_argument("--requests", type=int, default=10000, help="--workload serve: requests of the trace")
+    ap.add_argument("--serve-requests-compact", type=int, default=400, help="serve in the default line: requests")
+    ap.add_argument("--rate", type=float, default=12.0, help="serve: arrivals per second")
+    ap.add_argument("--serve-cycles", type=int, default=8, help="serve: cycles per round")
     ap.add_argument("--serve-waves", type=int, default=0,
-                    help="--workload serve: block waves the batches' schedules aim for (0 = autotuned)")
-    ap.add_argument("--plain-sample", type=int, default=100, help="--workload serve: requests timed on the plain path")
-    ap.add_argument("--accuracy-sample", type=int, default=5, help="--workload serve: FP32 requests checked against FP64")
+                    help="serve: block waves the batches' schedules aim for (0 = autotuned)")
+    ap.add_argument("--plain-sample", type=int, default=40, help="serve: requests timed on the plain path")
     ap.add_argument("--max-inflight", type=int, default=None,
-                    help="--workload serve: real cells running at once per batch (0 = no limit; default: the server's)")
+                    help="serve: real cells running at once per batch (0 = no limit; default: the server's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -91,12 +91,14 @@ typedef struct armon_solver_opts {
     int32_t unit_order;       /* 0 (default): each pass launches its blocks longest first, by the time
                                  each took in the previous cycle (results do not depend on it);
                                  -1: in index order */
-    int32_t split_pass;       /* 0 (default): each FP64 axis pass runs as two launches (face
-                                 fluxes, then the cell update), each keeping fewer values per thread
-                                 than one fused launch, so that more warps fit on an SM (fused when
-                                 the face buffer, 3 x max((nx+5) ny, (ny+5) nx) values, cannot be
-                                 allocated); FP32 passes stay fused.  1: split for either precision;
-                                 -1: fused.  Results are the same bits either way. */
+    int32_t split_pass;       /* 0 (default): an FP64 solver holds a face buffer (3 x max((nx+5) ny,
+                                 (ny+5) nx) values) and runs each axis pass as two launches (face
+                                 fluxes, then the cell update: fewer values per thread, more warps
+                                 per SM) or as one fused launch (half the bytes), whichever its
+                                 tiling measurement finds faster (domains under 2^20 cells: split;
+                                 fused when the face buffer cannot be allocated); FP32 passes stay
+                                 fused.  1: split for either precision; -1: fused.  Results are the
+                                 same bits either way. */
     int32_t reuse;            /* 0 (default): along each line, a position whose whole input window
                                  (the cells, and faces, its results depend on) repeats the previous
                                  position's bit for bit stores the previous position's results
@@ -154,13 +156,23 @@ int armon_solver_conservation(armon_solver* s, double* mass, double* energy);
 /* Number of kernels the solver launched so far (diagnostics). */
 int64_t armon_solver_kernel_launches(armon_solver* s);
 
-/* The tiling of the fused pass per axis (X, Y): cells per thread along the axis and blocks per
+/* The tiling of the axis pass per axis (X, Y): cells per thread along the axis and blocks per
  * launch.  Unless opts.seg_len fixes it, a domain of 2^20 cells or more gets the fastest of a few
- * candidate tilings, timed on its cycle-0 pass at the start of its first time loop (no change to
- * the state or the results); smaller domains use the cost model. */
+ * candidate tilings, each timed on real cycles of its first time loop (after 16 cycles with the
+ * model's tiling, two cycles per candidate forwards and two backwards: results never depend on
+ * the tiling), and cached per geometry for the process; smaller domains use the cost model. */
 int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2]);
 /* Lines (threads) per block of the fused pass: the caller's block_lines, or the measured choice. */
 int armon_solver_block_lines(const armon_solver* s);
+/* 1 while the time loop is still measuring candidate tilings on its cycles (domains of 2^20 cells
+ * or more whose geometry this process has not measured yet; results never depend on the tiling). */
+int armon_solver_tuning(const armon_solver* s);
+/* 1 when the axis passes run split (a face launch and a cell launch), 0 when fused: the caller's
+ * split_pass, or the measured form when split_pass is 0 and the solver holds a face buffer. */
+int armon_solver_split_pass(const armon_solver* s);
+/* Forgets the tilings measured so far in this process (the next time loop of each geometry
+ * measures again). */
+void armon_tiling_cache_clear(void);
 
 /* ---- batches: many independent domains advanced together (no counterpart in the reference;
  *      each domain follows time_loop, src/armon_2D.cpp:327-386, on its own) ---- */

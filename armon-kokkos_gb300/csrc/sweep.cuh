@@ -114,6 +114,11 @@ template <class T> constexpr int sweep_batch_cells_min_blocks() { return sizeof(
 #endif
 template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return ((ARMON_SWEEP_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 
+// Positions a run streams per iteration (loads issued together, then compared and stored).
+#ifndef ARMON_REUSE_BATCH
+#define ARMON_REUSE_BATCH 4
+#endif
+
 namespace armon {
 
 template <class T>
@@ -700,7 +705,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         // from the pipeline.
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = 2 * H;        // equal pairs that put a projection's window inside a run
-        constexpr int kReuseBatch = 4;
+        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
         __shared__ T run_slot[10][128];
         const int tid = threadIdx.x;
         const auto keep_run = [&](const CellIn<T>& c, const T (&o)[4]) {

@@ -166,7 +166,7 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         // are streamed, kReuseBatch at a time, and the march restarts from uniform_march(u).
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = kGAD ? 3 : 1;
-        constexpr int kReuseBatch = 4;
+        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
         // the run's state (rho, ua, uo, E, p, c) and uniform face (u*, p*, p* u*), kept in this
         // thread's slot of shared memory while the march computes
         __shared__ T run_slot[9][128];
@@ -402,7 +402,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
         // (the march's first Lagrange cell is t0, which reads faces t0 and t0 + 1).
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = 2 * LAG_A + 1;
-        constexpr int kReuseBatch = 4;
+        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
         // the run's unit (u*, p*, p* u*, rho, ua, uo, E) and uniform results (rho, ua, uo, E) in this
         // thread's slot of shared memory while the march computes; slots 11..14 hold the cell of the
         // previous step, which the next step compares with its own

@@ -700,6 +700,12 @@ int armon_solver_run(armon_solver* s, int cycle_limit)
             return ARMON_ERR_INVALID_DT;
         }
         bool running = st.time < s->cfg.max_time && st.cycle < s->cfg.max_cycles;
+        if (!running && s->tune.active) {
+            // the loop ended while measuring: the model's tiling, nothing cached
+            end_tuning(s);
+            rc = apply_tiling(s, model_tiling(s));
+            if (rc != ARMON_OK) return rc;
+        }
         if (!running || (cycle_limit > 0 && issued >= cycle_limit)) break;
         // at most the cycles left before max_cycles; when time decides, one graph batch at a time
         int left = s->cfg.max_cycles - st.cycle;

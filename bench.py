@@ -574,7 +574,8 @@ def batch_line(args, compact: bool) -> dict:
         s_, w_ = plain_solve(A, sp, 64, args.graph, args.block_lines, args.reuse)
         plain_secs += s_
         plain_work += w_
-    with A.Batch(precision=64, cycles_per_graph=8, block_lines=args.block_lines or 128, reuse=args.reuse) as b:
+    with A.Batch(precision=64, cycles_per_graph=8, block_lines=args.block_lines or 128, reuse=args.reuse,
+                 split_pass=args.split_pass) as b:
         ids = [b.add_sod(sp.params(), sp.sod_interface()) for sp in specs]
         b.poll()
         launches0 = b.kernel_launches

@@ -176,8 +176,8 @@ def test_invalid_dt_is_reported_not_fatal():
 
 
 def test_measured_tiling_keeps_results():
-    # a domain large enough for the solver to time its candidate tilings on the cycle-0 pass;
-    # whatever it picks, the cycles give the same bits as fixed tilings
+    # a domain large enough for the solver to time candidate tilings on its cycles (here only 4,
+    # before the measurement starts); whatever it runs, the cycles give the same bits as fixed tilings
     case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=1024, ny=1024, cfl=0.6,
                   max_cycles=4, max_time=1e9, test_option=0.04)
     out = []
@@ -217,25 +217,42 @@ def test_longest_first_dispatch_keeps_results(precision):
 
 
 @pytest.mark.parametrize("precision", [64, 32])
-def test_tiling_measured_on_developed_cycles_restores_the_state(precision):
-    # with room in the loop, the solver measures its candidate tilings on real cycles from a copy of
-    # the state and restarts from that copy: the run that follows equals one with a fixed tiling
+def test_tiling_measured_on_the_loops_own_cycles(precision):
+    # a domain of 2^20 cells or more times its candidate tilings (and, in FP64, pass forms) on the
+    # cycles of its own time loop: the results equal a fixed tiling's, the choice is cached for the
+    # geometry, and a loop that ends while measuring keeps the model's tiling and caches nothing
     case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=1024, ny=1040, cfl=0.6,
-                  max_cycles=200, max_time=1e9, test_option=0.04)
-    out = []
-    for seg in (0, 128):
-        with A.Solver(case, precision=precision, seg_len=seg) as s:
-            s.init_test()
-            p, status = s.state()
-            assert status == 0 and p.cycle == 0 and p.time == 0.0
-            s.run(cycle_limit=12)
-            p, status = s.state()
-            assert status == 0 and p.cycle == 12
-            out.append(({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt))
-    (a, ta, da), (b, tb, db) = out
-    assert ta == tb and da == db
+                  max_cycles=120, max_time=1e9, test_option=0.04)
+    A.tiling_cache_clear()
+    with A.Solver(case, precision=precision) as s:
+        s.init_test()
+        assert s.tuning()
+        s.run()
+        p, status = s.state()
+        assert status == 0 and p.cycle == 120 and not s.tuning()
+        got = ({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt)
+    with A.Solver(case, precision=precision) as s:
+        s.init_test()
+        assert not s.tuning()           # the cached choice
+    with A.Solver(case, precision=precision, seg_len=128) as s:
+        s.init_test()
+        assert not s.tuning()
+        s.run()
+        p, status = s.state()
+        ref = ({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt)
+    assert got[1:] == ref[1:]
     for k in FIELDS:
-        assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k
+        assert np.array_equal(got[0][k].view(np.int64), ref[0][k].view(np.int64)), k
+    A.tiling_cache_clear()
+    short = A.Case(**{**case.__dict__, "max_cycles": 30})
+    with A.Solver(short, precision=precision) as s:
+        s.init_test()
+        s.run()
+        p, status = s.state()
+        assert status == 0 and p.cycle == 30 and not s.tuning()
+    with A.Solver(short, precision=precision) as s:
+        s.init_test()
+        assert s.tuning()               # nothing was cached
 
 
 SPLIT_CASES = [

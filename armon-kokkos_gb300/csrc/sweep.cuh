@@ -767,15 +767,35 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             uniform_march(u);
         };
 
+        // The segment opens a run only when its first positions t0 .. t0 + 2H, the first
+        // projection's window, hold equal cells: loaded together, compared, and only then is the
+        // run's evaluation spent (a segment that starts in a front computes from t0 at once).
+        const auto opens_run = [&](const CellIn<T>& c) {
+            bool same[kEnter];
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) {
+                int m, side;
+                const bool stale = source(t0 + 1 + q, m, side);
+                const int64_t idx = base + (int64_t)m * s;
+                CellIn<T> cq;
+                cq.rho = rho_in[idx]; cq.ua = ua_in[idx]; cq.uo = uo_in[idx]; cq.E = E_in[idx];
+                mirror(cq, side);
+                same[q] = !stale && same_state(cq, c);
+            }
+            bool all = true;
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) all = all && same[q];
+            return all;
+        };
         int t = t0;
         if (reuse) {
             int m, side;
             const bool stale = source(t0, m, side);
-            if (!stale) {
-                const int64_t idx = base + (int64_t)m * s;
-                CellIn<T> c;
-                c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
-                mirror(c, side);
+            const int64_t idx = base + (int64_t)m * s;
+            CellIn<T> c;
+            c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+            mirror(c, side);
+            if (!stale && opens_run(c)) {
                 prepare(c);
                 uniform_march(c);
                 T o[4];

@@ -218,13 +218,30 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
             uniform_march(u);
         };
 
+        // the segment opens a run only when cells t0 .. t0 + kEnter, the first face's window, are
+        // equal (loaded together and compared before the run's evaluation is spent)
+        const auto opens_run = [&](const CellIn<T>& c) {
+            bool same[kEnter];
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) {
+                CellIn<T> cq;
+                int mq;
+                int64_t iq;
+                const bool stale = load_position(g, n, sw, base, t0 + 1 + q, rho_in, ua_in, uo_in, E_in, cq, mq, iq);
+                same[q] = !stale && same_state(cq, c);
+            }
+            bool all = true;
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) all = all && same[q];
+            return all;
+        };
         int t = t0;
         int run = 0;
         if (reuse) {
             CellIn<T> c;
             int m;
             int64_t idx;
-            if (!load_position(g, n, sw, base, t0, rho_in, ua_in, uo_in, E_in, c, m, idx)) {
+            if (!load_position(g, n, sw, base, t0, rho_in, ua_in, uo_in, E_in, c, m, idx) && opens_run(c)) {
                 prepare(c);
                 uniform_march(c);
                 T o[3];
@@ -456,14 +473,29 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
 
         int t = t0;
         int run = 0;
-        if (reuse) {
+        // units t0 + 2 .. t0 + 1 + kEnter must equal it too (loaded together) before the run's
+        // evaluation is spent; they lie in the segment's range (faces up to t1) when
+        // t1 - t0 = b0 - a0 + 2 LAG_A >= kEnter + 1, i.e. for segments of two cells or more
+        if (reuse && t1 - t0 >= kEnter + 1) {
             Flux<T> f0, f1;
             CellIn<T> c;
             load_face(t0, f0);
             load_face(t0 + 1, f1);
             load_cell(t0, c);
-            if (same_bits(f0.us, f1.us) & same_bits(f0.ps, f1.ps) & same_bits(f0.psus, f1.psus)) {
-                const Unit v{f1, c};
+            const Unit v{f1, c};
+            bool same[kEnter];
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) {
+                Flux<T> fq;
+                CellIn<T> cq;
+                load_face(t0 + 2 + q, fq);
+                load_cell(t0 + 1 + q, cq);
+                same[q] = same_unit(fq, cq, v);
+            }
+            bool all = same_bits(f0.us, f1.us) & same_bits(f0.ps, f1.ps) & same_bits(f0.psus, f1.psus);
+#pragma unroll
+            for (int q = 0; q < kEnter; q++) all = all && same[q];
+            if (all) {
                 uniform_march(v);
                 T o[4];
                 project(kE2 ? L1 : L2, A0, A1, o);

@@ -243,13 +243,14 @@ def test_tiling_measured_on_the_loops_own_cycles(precision):
     assert got[1:] == ref[1:]
     for k in FIELDS:
         assert np.array_equal(got[0][k].view(np.int64), ref[0][k].view(np.int64)), k
+    # 20 cycles: the measurement starts after 16 and needs at least two per candidate
     A.tiling_cache_clear()
-    short = A.Case(**{**case.__dict__, "max_cycles": 30})
+    short = A.Case(**{**case.__dict__, "max_cycles": 20})
     with A.Solver(short, precision=precision) as s:
         s.init_test()
         s.run()
         p, status = s.state()
-        assert status == 0 and p.cycle == 30 and not s.tuning()
+        assert status == 0 and p.cycle == 20 and not s.tuning()
     with A.Solver(short, precision=precision) as s:
         s.init_test()
         assert s.tuning()               # nothing was cached

@@ -567,7 +567,8 @@ def batch_line(args, compact: bool) -> dict:
 
     specs = W.mixed_domains(args.domains, seed=2024)
     torch.cuda.set_device(0)
-    sample = stratified(specs, lambda sp: sp.nx * sp.ny, args.plain_domains) if compact else specs
+    n_plain = args.plain_domains or (32 if compact else len(specs))
+    sample = stratified(specs, lambda sp: sp.nx * sp.ny, n_plain)
     plain_solve(A, sample[0], 64, args.graph, args.block_lines, args.reuse)   # warm-up
     plain_secs, plain_work = 0.0, 0
     for sp in sample:
@@ -701,10 +702,14 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
                     help="single: the 4096^2 drop-in case (default); batch: 256 mixed domains; serve: a request trace")
     ap.add_argument("--domains", type=int, default=256, help="batch: domains")
-    ap.add_argument("--plain-domains", type=int, default=32, help="batch in the default line: domains timed on the plain path")
+    ap.add_argument("--plain-domains", type=int, default=0,
+                    help="batch: domains timed on the plain path, a stratified sample (0 = 32 in the default line, "
+                         "all with --workload batch)")
     ap.add_argument("--requests", type=int, default=10000, help="--workload serve: requests of the trace")
-    ap.add_argument("--serve-requests-compact", type=int, default=400, help="serve in the default line: requests")
-    ap.add_argument("--rate", type=float, default=12.0, help="serve: arrivals per second")
+    ap.add_argument("--serve-requests-compact", type=int, default=600, help="serve in the default line: requests")
+    ap.add_argument("--rate", type=float, default=50.0,
+                    help="serve: arrivals per second (50 offers more than one GB300 serves, so the served rate "
+                         "is the server's capacity)")
     ap.add_argument("--serve-cycles", type=int, default=8, help="serve: cycles per round")
     ap.add_argument("--serve-waves", type=int, default=0,
                     help="serve: block waves the batches' schedules aim for (0 = autotuned)")

@@ -114,10 +114,23 @@ template <class T> constexpr int sweep_batch_cells_min_blocks() { return sizeof(
 #endif
 template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return ((ARMON_SWEEP_PREFETCH >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 
-// Positions a run streams per iteration (loads issued together, then compared and stored).
+// Positions a run streams per iteration (loads issued together, then compared and stored), FP64
+// and FP32, and how many batches ahead the streaming loop asks L2 for the lines it will load next
+// (prefetch.global.L2: no registers, no data returned; 0 = none).
 #ifndef ARMON_REUSE_BATCH
 #define ARMON_REUSE_BATCH 4
 #endif
+#ifndef ARMON_REUSE_BATCH_F32
+#define ARMON_REUSE_BATCH_F32 4
+#endif
+#ifndef ARMON_REUSE_PREFETCH
+#define ARMON_REUSE_PREFETCH 1
+#endif
+template <class T> __host__ __device__ constexpr int reuse_batch() { return sizeof(T) == 8 ? ARMON_REUSE_BATCH : ARMON_REUSE_BATCH_F32; }
+constexpr int kReusePrefetch = ARMON_REUSE_PREFETCH;
+
+// A hint that the line holding p will be read soon: L2 fetches it; nothing comes back to the thread.
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 namespace armon {
 
@@ -705,7 +718,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
         // from the pipeline.
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = 2 * H;        // equal pairs that put a projection's window inside a run
-        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
+        constexpr int kReuseBatch = reuse_batch<T>();
         __shared__ T run_slot[10][128];
         const int tid = threadIdx.x;
         const auto keep_run = [&](const CellIn<T>& c, const T (&o)[4]) {
@@ -736,6 +749,17 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                         c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
                         mirror(c, side);
                         same[q] = !stale && same_state(c, u);
+                    }
+                }
+                // the lines of the batches that follow, positions the march reads (at most t1)
+#pragma unroll
+                for (int q = 0; q < kReusePrefetch * kReuseBatch; q++) {
+                    const int tp = t + nb + q;
+                    if (tp <= t1) {
+                        int m, side;
+                        source(tp, m, side);
+                        const int64_t idx = base + (int64_t)m * s;
+                        prefetch_l2(rho_in + idx); prefetch_l2(ua_in + idx); prefetch_l2(uo_in + idx); prefetch_l2(E_in + idx);
                     }
                 }
                 int k = 0;

@@ -47,6 +47,15 @@ __device__ __forceinline__ UnitPos unit_position(const AxisGeom<T>& g, const uin
     return p;
 }
 
+// The cell of the line that position tt reads: itself, or the real cell it mirrors.
+template <class T>
+__device__ __forceinline__ int position_source(const AxisGeom<T>&, int n, int sw, int tt)
+{
+    if (tt < 0 && tt >= -sw) return -1 - tt;
+    if (tt >= n && tt < n + sw) return 2 * n - 1 - tt;
+    return tt;
+}
+
 // The cell at position tt of a line: the real cell itself, a mirror of a real cell (side 1: low
 // side, 2: high side) with the boundary's sign factors, or an untouched ghost (stale: true).
 template <class T>
@@ -166,7 +175,7 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         // are streamed, kReuseBatch at a time, and the march restarts from uniform_march(u).
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = kGAD ? 3 : 1;
-        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
+        constexpr int kReuseBatch = reuse_batch<T>();
         // the run's state (rho, ua, uo, E, p, c) and uniform face (u*, p*, p* u*), kept in this
         // thread's slot of shared memory while the march computes
         __shared__ T run_slot[9][128];
@@ -198,6 +207,15 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
                         int64_t idx;
                         const bool stale = load_position(g, n, sw, base, t + q, rho_in, ua_in, uo_in, E_in, c, m, idx);
                         same[q] = !stale && same_state(c, u);
+                    }
+                }
+                // the lines of the batches that follow, positions the march reads (at most t1)
+#pragma unroll
+                for (int q = 0; q < kReusePrefetch * kReuseBatch; q++) {
+                    const int tp = t + nb + q;
+                    if (tp <= t1) {
+                        const int64_t idx = base + (int64_t)position_source(g, n, sw, tp) * g.s;
+                        prefetch_l2(rho_in + idx); prefetch_l2(ua_in + idx); prefetch_l2(uo_in + idx); prefetch_l2(E_in + idx);
                     }
                 }
                 int k = 0;
@@ -419,7 +437,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
         // (the march's first Lagrange cell is t0, which reads faces t0 and t0 + 1).
         const bool reuse = A.reuse != 0;
         constexpr int kEnter = 2 * LAG_A + 1;
-        constexpr int kReuseBatch = ARMON_REUSE_BATCH;
+        constexpr int kReuseBatch = reuse_batch<T>();
         // the run's unit (u*, p*, p* u*, rho, ua, uo, E) and uniform results (rho, ua, uo, E) in this
         // thread's slot of shared memory while the march computes; slots 11..14 hold the cell of the
         // previous step, which the next step compares with its own
@@ -453,6 +471,17 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
                         load_face(t + q, f);
                         load_cell(t + q - 1, c);
                         same[q] = same_unit(f, c, v);
+                    }
+                }
+                // the lines of the batches that follow, positions the march reads (at most t1)
+#pragma unroll
+                for (int q = 0; q < kReusePrefetch * kReuseBatch; q++) {
+                    const int tp = t + nb + q;
+                    if (tp <= t1) {
+                        const int64_t fi = face_index(g, tp, P.line);
+                        prefetch_l2(us_in + fi); prefetch_l2(ps_in + fi); prefetch_l2(psus_in + fi);
+                        const int64_t idx = base + (int64_t)position_source(g, n, sw, tp - 1) * g.s;
+                        prefetch_l2(rho_in + idx); prefetch_l2(ua_in + idx); prefetch_l2(uo_in + idx); prefetch_l2(E_in + idx);
                     }
                 }
                 int k = 0;

@@ -116,7 +116,10 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 
 // Positions a run streams per iteration (loads issued together, then compared and stored), FP64
 // and FP32, and how many batches ahead the streaming loop asks L2 for the lines it will load next
-// (prefetch.global.L2: no registers, no data returned; 0 = none).
+// (prefetch.global.L2: no registers, no data returned; 0 = none).  Measured at 4096² FP64 / 8192²
+// FP32, cycles 180-200 / 80-100 (G cell-updates/s): no prefetch 6.78 / 13.84, one batch ahead
+// 6.47 / 12.77, two 5.85 / 10.32; FP32 batches of 8: 12.72 (one ahead); FP64 batches of 8 or 16
+// (no prefetch): 6.41, 6.15.
 #ifndef ARMON_REUSE_BATCH
 #define ARMON_REUSE_BATCH 4
 #endif
@@ -124,7 +127,7 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 #define ARMON_REUSE_BATCH_F32 4
 #endif
 #ifndef ARMON_REUSE_PREFETCH
-#define ARMON_REUSE_PREFETCH 1
+#define ARMON_REUSE_PREFETCH 0
 #endif
 template <class T> __host__ __device__ constexpr int reuse_batch() { return sizeof(T) == 8 ? ARMON_REUSE_BATCH : ARMON_REUSE_BATCH_F32; }
 constexpr int kReusePrefetch = ARMON_REUSE_PREFETCH;

@@ -738,20 +738,51 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             u.rho = run_slot[0][tid]; u.ua = run_slot[1][tid]; u.uo = run_slot[2][tid]; u.E = run_slot[3][tid];
             const T up = run_slot[4][tid], uc = run_slot[5][tid];
             const T u_out[4] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid], run_slot[9][tid]};
+            const bool pcg_out = LAST || A.write_eos;
             while (t <= t1) {
                 const int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];
+                if (nb == kReuseBatch && t >= a0 && t + kReuseBatch <= b0 && t - H >= a0) {
+                    // a batch of real cells the segment owns, each with a result to store: no mirror,
+                    // no ghost, and the stores need no per-position test
 #pragma unroll
-                for (int q = 0; q < kReuseBatch; q++) {
-                    same[q] = false;
-                    if (q < nb) {
-                        int m, side;
-                        const bool stale = source(t + q, m, side);
-                        const int64_t idx = base + (int64_t)m * s;
+                    for (int q = 0; q < kReuseBatch; q++) {
+                        const int64_t idx = base + (int64_t)(t + q) * s;
                         CellIn<T> c;
                         c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
-                        mirror(c, side);
-                        same[q] = !stale && same_state(c, u);
+                        same[q] = same_state(c, u);
+                    }
+                    bool all = true;
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
+                    if (all) {
+#pragma unroll
+                        for (int q = 0; q < kReuseBatch; q++) {
+                            if (pcg_out) {
+                                const int64_t idx = base + (int64_t)(t + q) * s;
+                                A.pmat[idx] = up;
+                                A.cmat[idx] = uc;
+                                A.gmat[idx] = (1 + A.gamma) / 2;
+                            }
+                            store_out(t + q - H, u_out);
+                        }
+                        if (LAST && !counted) { add_dt(u_out, uc); counted = true; }
+                        t += kReuseBatch;
+                        continue;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) {
+                        same[q] = false;
+                        if (q < nb) {
+                            int m, side;
+                            const bool stale = source(t + q, m, side);
+                            const int64_t idx = base + (int64_t)m * s;
+                            CellIn<T> c;
+                            c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                            mirror(c, side);
+                            same[q] = !stale && same_state(c, u);
+                        }
                     }
                 }
                 // the lines of the batches that follow, positions the march reads (at most t1)
@@ -770,7 +801,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 for (int q = 0; q < kReuseBatch; q++) k += (k == q && same[q]) ? 1 : 0;
                 for (int q = 0; q < k; q++) {
                     const int tt = t + q;
-                    if (tt >= a0 && tt < b0 && (LAST || A.write_eos)) {   // owned real cell
+                    if (tt >= a0 && tt < b0 && pcg_out) {   // owned real cell
                         const int64_t idx = base + (int64_t)tt * s;
                         A.pmat[idx] = up;
                         A.cmat[idx] = uc;

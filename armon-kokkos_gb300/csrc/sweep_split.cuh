@@ -195,18 +195,48 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         const auto stream = [&](int t) -> int {
             const CellIn<T> u = run_cell();
             const T u_out[3] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid]};
+            const bool pcg_out = LAST || A.write_eos;
             while (t <= t1) {
                 const int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];
+                if (nb == kReuseBatch && t >= a0 && t + kReuseBatch <= b0 && t >= t0 + 1 + 2 * LAGF) {
+                    // a batch of real cells the segment owns, each ending a face to store: no mirror,
+                    // no ghost, and the stores need no per-position test
 #pragma unroll
-                for (int q = 0; q < kReuseBatch; q++) {
-                    same[q] = false;
-                    if (q < nb) {
+                    for (int q = 0; q < kReuseBatch; q++) {
+                        const int64_t idx = base + (int64_t)(t + q) * g.s;
                         CellIn<T> c;
-                        int m;
-                        int64_t idx;
-                        const bool stale = load_position(g, n, sw, base, t + q, rho_in, ua_in, uo_in, E_in, c, m, idx);
-                        same[q] = !stale && same_state(c, u);
+                        c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                        same[q] = same_state(c, u);
+                    }
+                    bool all = true;
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
+                    if (all) {
+#pragma unroll
+                        for (int q = 0; q < kReuseBatch; q++) {
+                            if (pcg_out) {
+                                const int64_t idx = base + (int64_t)(t + q) * g.s;
+                                A.pmat[idx] = u.p;
+                                A.cmat[idx] = u.c;
+                                A.gmat[idx] = (1 + A.gamma) / 2;
+                            }
+                            store_face(t + q - LAGF, u_out);
+                        }
+                        t += kReuseBatch;
+                        continue;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) {
+                        same[q] = false;
+                        if (q < nb) {
+                            CellIn<T> c;
+                            int m;
+                            int64_t idx;
+                            const bool stale = load_position(g, n, sw, base, t + q, rho_in, ua_in, uo_in, E_in, c, m, idx);
+                            same[q] = !stale && same_state(c, u);
+                        }
                     }
                 }
                 // the lines of the batches that follow, positions the march reads (at most t1)
@@ -462,15 +492,38 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs<T>& A, const int blk
             while (t <= t1) {
                 const int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];
+                if (nb == kReuseBatch && t - 1 >= 0 && t + kReuseBatch - 1 <= n && t - LAG_A - 1 >= a0) {
+                    // units of real cells, each with a result to store: no mirror, no per-position test
 #pragma unroll
-                for (int q = 0; q < kReuseBatch; q++) {
-                    same[q] = false;
-                    if (q < nb) {
+                    for (int q = 0; q < kReuseBatch; q++) {
                         Flux<T> f;
                         CellIn<T> c;
                         load_face(t + q, f);
-                        load_cell(t + q - 1, c);
+                        const int64_t idx = base + (int64_t)(t + q - 1) * s;
+                        c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
                         same[q] = same_unit(f, c, v);
+                    }
+                    bool all = true;
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
+                    if (all) {
+#pragma unroll
+                        for (int q = 0; q < kReuseBatch; q++) store_out(t + q - LAG_A - 1, v_out);
+                        if (LAST && !counted) { add_dt(t - LAG_A - 1, v_out); counted = true; }
+                        t += kReuseBatch;
+                        continue;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kReuseBatch; q++) {
+                        same[q] = false;
+                        if (q < nb) {
+                            Flux<T> f;
+                            CellIn<T> c;
+                            load_face(t + q, f);
+                            load_cell(t + q - 1, c);
+                            same[q] = same_unit(f, c, v);
+                        }
                     }
                 }
                 // the lines of the batches that follow, positions the march reads (at most t1)

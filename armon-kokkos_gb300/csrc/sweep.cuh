@@ -132,6 +132,23 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 template <class T> __host__ __device__ constexpr int reuse_batch() { return sizeof(T) == 8 ? ARMON_REUSE_BATCH : ARMON_REUSE_BATCH_F32; }
 constexpr int kReusePrefetch = ARMON_REUSE_PREFETCH;
 
+// Two consecutive values with one 8-byte (float) or 16-byte (double) access; p must be aligned to
+// two values.
+__device__ __forceinline__ void load2(const float* p, float& a, float& b)
+{
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    a = v.x;
+    b = v.y;
+}
+__device__ __forceinline__ void load2(const double* p, double& a, double& b)
+{
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    a = v.x;
+    b = v.y;
+}
+__device__ __forceinline__ void store2(float* p, float v) { *reinterpret_cast<float2*>(p) = make_float2(v, v); }
+__device__ __forceinline__ void store2(double* p, double v) { *reinterpret_cast<double2*>(p) = make_double2(v, v); }
+
 // A hint that the line holding p will be read soon: L2 fetches it; nothing comes back to the thread.
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
@@ -739,32 +756,79 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             const T up = run_slot[4][tid], uc = run_slot[5][tid];
             const T u_out[4] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid], run_slot[9][tid]};
             const bool pcg_out = LAST || A.write_eos;
+            const T g_out = (1 + A.gamma) / 2;
+            // Along a row (s == 1) the cells of a batch are consecutive in memory: when every array's
+            // address of the batch's first cell (and of its first result) is aligned to two values, the
+            // batch moves pairs of cells with one access each, half the requests of a warp whose 32
+            // threads each walk their own row.  With an even row length every thread of the warp has
+            // the same alignment, so no thread waits for another.
+            const auto pair_aligned = [&](int tt) {
+                constexpr uintptr_t mask = 2 * sizeof(T) - 1;
+                const int64_t i = base + tt, o = base + tt - H;
+                uintptr_t a = (uintptr_t)(rho_in + i) | (uintptr_t)(ua_in + i) | (uintptr_t)(uo_in + i) |
+                              (uintptr_t)(E_in + i) | (uintptr_t)(out[0] + o) | (uintptr_t)(out[1] + o) |
+                              (uintptr_t)(out[2] + o) | (uintptr_t)(out[3] + o);
+                if (pcg_out) a |= (uintptr_t)(A.pmat + i) | (uintptr_t)(A.cmat + i) | (uintptr_t)(A.gmat + i);
+                return (a & mask) == 0;
+            };
             while (t <= t1) {
-                const int nb = min(kReuseBatch, t1 - t + 1);
+                int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];
-                if (nb == kReuseBatch && t >= a0 && t + kReuseBatch <= b0 && t - H >= a0) {
+                bool fast = nb == kReuseBatch && t >= a0 && t + kReuseBatch <= b0 && t - H >= a0;
+                bool pairs = false;
+                if (fast && s == 1 && kReuseBatch % 2 == 0) {
+                    pairs = pair_aligned(t);
+                    if (!pairs && pair_aligned(t + 1)) { fast = false; nb = 1; }   // one position to the alignment
+                }
+                if (fast) {
                     // a batch of real cells the segment owns, each with a result to store: no mirror,
                     // no ghost, and the stores need no per-position test
+                    if (pairs) {
 #pragma unroll
-                    for (int q = 0; q < kReuseBatch; q++) {
-                        const int64_t idx = base + (int64_t)(t + q) * s;
-                        CellIn<T> c;
-                        c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
-                        same[q] = same_state(c, u);
+                        for (int q = 0; q < kReuseBatch; q += 2) {
+                            const int64_t idx = base + t + q;
+                            CellIn<T> c0, c1;
+                            load2(rho_in + idx, c0.rho, c1.rho);
+                            load2(ua_in + idx, c0.ua, c1.ua);
+                            load2(uo_in + idx, c0.uo, c1.uo);
+                            load2(E_in + idx, c0.E, c1.E);
+                            same[q] = same_state(c0, u);
+                            same[q + 1] = same_state(c1, u);
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < kReuseBatch; q++) {
+                            const int64_t idx = base + (int64_t)(t + q) * s;
+                            CellIn<T> c;
+                            c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                            same[q] = same_state(c, u);
+                        }
                     }
                     bool all = true;
 #pragma unroll
                     for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
                     if (all) {
+                        if (pairs) {
 #pragma unroll
-                        for (int q = 0; q < kReuseBatch; q++) {
-                            if (pcg_out) {
-                                const int64_t idx = base + (int64_t)(t + q) * s;
-                                A.pmat[idx] = up;
-                                A.cmat[idx] = uc;
-                                A.gmat[idx] = (1 + A.gamma) / 2;
+                            for (int q = 0; q < kReuseBatch; q += 2) {
+                                const int64_t i = base + t + q, o = i - H;
+                                if (pcg_out) { store2(A.pmat + i, up); store2(A.cmat + i, uc); store2(A.gmat + i, g_out); }
+                                store2(out[0] + o, u_out[0]);
+                                store2(out[axis == 0 ? 1 : 2] + o, u_out[1]);
+                                store2(out[axis == 0 ? 2 : 1] + o, u_out[2]);
+                                store2(out[3] + o, u_out[3]);
                             }
-                            store_out(t + q - H, u_out);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < kReuseBatch; q++) {
+                                if (pcg_out) {
+                                    const int64_t idx = base + (int64_t)(t + q) * s;
+                                    A.pmat[idx] = up;
+                                    A.cmat[idx] = uc;
+                                    A.gmat[idx] = g_out;
+                                }
+                                store_out(t + q - H, u_out);
+                            }
                         }
                         if (LAST && !counted) { add_dt(u_out, uc); counted = true; }
                         t += kReuseBatch;

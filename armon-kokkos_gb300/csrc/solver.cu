@@ -1,9 +1,10 @@
 // solver.cu -- the native solver: device-resident state, the fused time loop and its C ABI
 // (include/armon_gb300.h).
 //
-// One cycle = passes_per_cycle(splitting) launches of the fused sweep; the last one also reduces
-// dt_CFL of the new state and commits the cycle (time, cycle, dts) into the device StepState, so
-// the host never waits inside the loop.  Cycles are issued in batches captured in a CUDA graph;
+// One cycle = passes_per_cycle(splitting) axis passes, each one fused launch or a face and a cell
+// launch (the tiling measurement picks the form); the last one also reduces dt_CFL of the new
+// state and commits the cycle (time, cycle, dts) into the device StepState, so the host never
+// waits inside the loop.  Cycles are issued in batches captured in a CUDA graph;
 // after each batch the host reads the 48-byte state back to test the reference's loop condition
 // (time < max_time && cycle < max_cycles).  Cycles issued past the end are no-ops on the device.
 #include <algorithm>

@@ -1,9 +1,8 @@
 """Parity at the benchmark configurations, against the strict oracle.
 
 * Circular Sod at 4096 x 4096 (radius 0.2, GAD-minmod, second-order remap, CFL 0.6, FP64) run the way
-  the benchmark runs it: default options, so the tiling is measured on developed cycles, units are
-  dispatched longest first, each FP64 pass is split and runs of identical inputs reuse their
-  results.  Every cycle's dt and time equal the oracle's as doubles and the final rho, u, v, E, p, c
+  the benchmark runs it: default options, so the tiling and pass form are measured on the loop's
+  own cycles, units are dispatched longest first and runs of identical inputs reuse their results.  Every cycle's dt and time equal the oracle's as doubles and the final rho, u, v, E, p, c
   hash the same, for a cycle-by-cycle run and for a run in CUDA-graph batches.  The same at 2048^2
   over 120 cycles, where the fronts have moved some 60 cells.
 * The FP32 variant at 8192 x 8192 against the FP64 oracle: L1 relative error of rho and E, and the

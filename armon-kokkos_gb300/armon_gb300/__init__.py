@@ -237,7 +237,7 @@ class Solver:
     """A domain resident in HBM with the fused time loop (armon_solver_* of include/armon_gb300.h)."""
 
     def __init__(self, params: Params | Case, precision: int = 64, stream: int | None = None,
-                 cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = 0,
+                 cycles_per_graph: int = 16, seg_len: int = 0, block_lines: int = 0, materialize_eos: int = -1,
                  unit_order: int = 0, split_pass: int = 0, reuse: int = 0):
         L = lib()
         self.params = make_params(params) if isinstance(params, Case) else params

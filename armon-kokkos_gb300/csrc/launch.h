@@ -90,6 +90,7 @@ struct BeginArgs {
     StepConfig cfg;
     double* partials;
     int32_t buf_base;
+    int32_t eos_only;   // 1: only p, c, g of the real cells from rho, umat, vmat, Emat (no dt, no state)
 };
 cudaError_t launch_begin_f64(const BeginArgs& a, int grid, cudaStream_t st);
 cudaError_t launch_begin_f32(const BeginArgs& a, int grid, cudaStream_t st);

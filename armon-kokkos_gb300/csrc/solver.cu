@@ -66,6 +66,7 @@ struct armon_solver {
         std::array<int, 9> key{};
     } tune;
     int64_t issued = 0;             // cycles issued since begin_loop
+    bool eos_stale = false;         // p, c, g of the last pass's input are not in memory yet
     double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
     bool ordered = true;            // longest-first dispatch of each pass's units
     uint32_t* d_order = nullptr;    // per axis: order_cap unit indices, then order_cap costs
@@ -99,8 +100,11 @@ void fill_geom(armon_solver* s, SweepArgs<T>& a)
     DomainBuffers<T> b{{{arr[2], arr[3], arr[4], arr[5]}, {arr[11], arr[12], arr[13], arr[14]}}, arr[6], arr[7], arr[8]};
     const int forced[2] = {s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[0],
                            s->o.seg_len > 0 ? s->o.seg_len : s->tuned_seg[1]};
+    // the split form's cell half reads c of the last pass's cells (dt_CFL), so its face half writes
+    // p, c, g on the last pass at least
+    const int eos = s->split ? std::max(0, s->o.materialize_eos) : s->o.materialize_eos;
     s->grid = make_sweep_args<T>(s->p, s->npass, s->block, s->sm_count, forced, b, s->d_state, s->d_partials,
-                                 s->o.materialize_eos, s->o.reuse >= 0 ? 1 : 0, a);
+                                 eos, s->o.reuse >= 0 ? 1 : 0, a);
     if (s->split) {
         a.faces = static_cast<T*>(s->d_faces);
         a.face_stride = s->face_stride;
@@ -190,6 +194,7 @@ cudaError_t launch_pass(armon_solver* s, int k, bool last)
 
 int enqueue_direct(armon_solver* s, int n_cycles)
 {
+    if (n_cycles > 0) s->eos_stale = !s->split && s->o.materialize_eos < 0;
     for (int c = 0; c < n_cycles; c++) {
         for (int k = 0; k < s->npass; k++) {
             bool last = k == s->npass - 1;
@@ -224,6 +229,7 @@ int build_graph(armon_solver* s)
 int enqueue_steady(armon_solver* s, int n_cycles)
 {
     s->issued += n_cycles;
+    if (n_cycles > 0) s->eos_stale = !s->split && s->o.materialize_eos < 0;
     if (s->graph_cycles > 0 && n_cycles >= s->graph_cycles) {
         int rc = build_graph(s);
         if (rc != ARMON_OK) return rc;
@@ -489,10 +495,38 @@ int enqueue(armon_solver* s, int n_cycles)
     return enqueue_steady(s, n_cycles);
 }
 
+// p, c, g as update_EOS left them: the EOS of the last pass's input, which the set the current
+// state is not in still holds (every pass reads one set and writes the other).  Passes that do not
+// store them (materialize_eos < 0) leave this to the moment they are read, the loop ends, or the
+// state is settled.
+int materialize_eos(armon_solver* s)
+{
+    if (!s->eos_stale) return ARMON_OK;
+    CUDA_TRY(cudaMemcpyAsync(s->h_state, s->d_state, sizeof(StepState), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const StepState& st = *s->h_state;
+    const int cur = (int)(((int64_t)st.cycle * s->npass + st.buf_base) & 1);
+    const int in = cur ^ 1;                      // the set the last pass read
+    BeginArgs b{};
+    b.nx = s->p.nx; b.ny = s->p.ny;
+    b.origin = (int64_t)s->p.nb_ghosts * s->p.row_length + s->p.nb_ghosts;
+    b.row_length = s->p.row_length;
+    b.gamma = 1.4;
+    b.rho = s->arr[in ? 11 : 2]; b.umat = s->arr[in ? 12 : 3]; b.vmat = s->arr[in ? 13 : 4]; b.Emat = s->arr[in ? 14 : 5];
+    b.pmat = s->arr[6]; b.cmat = s->arr[7]; b.gmat = s->arr[8];
+    b.eos_only = 1;
+    CUDA_TRY(launch_begin(b, s->fp32, s->sm_count * 4, s->stream));
+    s->launches++;
+    s->eos_stale = false;
+    return ARMON_OK;
+}
+
 // Puts the current state back into set 0 (rho, umat, vmat, Emat) so that the reference's
 // arrays hold it, as after the reference's time loop.
 int settle(armon_solver* s)
 {
+    int rc = materialize_eos(s);
+    if (rc != ARMON_OK) return rc;
     const StepState& st = *s->h_state;
     int cur = (int)(((int64_t)st.cycle * s->npass + st.buf_base) & 1);
     if (cur == 0) return ARMON_OK;
@@ -515,7 +549,7 @@ void armon_solver_opts_default(armon_solver_opts* o)
     std::memset(o, 0, sizeof(*o));
     o->precision = 64;
     o->cycles_per_graph = 16;
-    o->materialize_eos = 0;
+    o->materialize_eos = -1;
 }
 
 static int solver_create(const armon_params* p, const armon_solver_opts* opts, double* const* borrowed, void* stream,
@@ -657,6 +691,7 @@ int armon_solver_begin_loop(armon_solver* s)
     CUDA_TRY(launch_begin(b, s->fp32, s->sm_count * 4, s->stream));
     s->launches++;
     s->begun = true;
+    s->eos_stale = false;
     s->issued = 0;
     int rc = sync_state(s);
     if (rc == ARMON_OK) rc = start_tuning(s);
@@ -747,7 +782,8 @@ static int current_index(armon_solver* s, int which)
 int armon_solver_download(armon_solver* s, int which, double* host)
 {
     if (which < 0 || which > 15) { set_error("array index out of range"); return ARMON_ERR_PARAMS; }
-    int rc = sync_state(s);
+    int rc = (which >= 6 && which <= 8) ? materialize_eos(s) : ARMON_OK;
+    if (rc == ARMON_OK) rc = sync_state(s);
     if (rc != ARMON_OK) return rc;
     int k = current_index(s, which);
     size_t n = (size_t)s->p.nb_cells;
@@ -769,7 +805,8 @@ int armon_solver_download(armon_solver* s, int which, double* host)
 int armon_solver_upload(armon_solver* s, int which, const double* host)
 {
     if (which < 0 || which > 15) { set_error("array index out of range"); return ARMON_ERR_PARAMS; }
-    int rc = sync_state(s);
+    int rc = (which >= 6 && which <= 8) ? materialize_eos(s) : ARMON_OK;
+    if (rc == ARMON_OK) rc = sync_state(s);
     if (rc != ARMON_OK) return rc;
     int k = current_index(s, which);
     size_t n = (size_t)s->p.nb_cells;
@@ -791,6 +828,7 @@ int armon_solver_upload(armon_solver* s, int which, const double* host)
 double* armon_solver_device_array(armon_solver* s, int which)
 {
     if (s->fp32 || which < 0 || which > 15) return nullptr;
+    if (which >= 6 && which <= 8 && materialize_eos(s) != ARMON_OK) return nullptr;
     if (sync_state(s) != ARMON_OK) return nullptr;
     return (double*)s->arr[current_index(s, which)];
 }

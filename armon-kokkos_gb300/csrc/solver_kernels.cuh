@@ -65,7 +65,9 @@ template <class T>
 __global__ void begin_kernel(BeginArgs a)
 {
     // update_EOS on the real cells (src/armon_2D.cpp:85-101, src/kernels/fluid_eos.cpp:9-23) and
-    // the dt_CFL of that state for cycle 0.
+    // the dt_CFL of that state for cycle 0 (eos_only: the EOS alone).  The same IEEE operations in
+    // the same order as the axis pass's EOS (u^2 + v^2 and v^2 + u^2 are the same sum), so the values
+    // are the same bits.
     DtAcc acc;
     acc.init();
     const int64_t nreal = (int64_t)a.nx * a.ny;
@@ -83,6 +85,7 @@ __global__ void begin_kernel(BeginArgs a)
         gmat[idx] = (1 + gamma) / 2;
         acc.add(umat[idx], vmat[idx], c);
     }
+    if (a.eos_only) return;
     acc.finish();
     double gx, gy;
     if (grid_dt_maxima(acc, a.partials, &a.state->counter, &gx, &gy)) {

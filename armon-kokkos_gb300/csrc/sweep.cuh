@@ -188,7 +188,8 @@ struct SweepArgs {
     int32_t limiter;                  // 0 None, 1 Minmod, 2 Superbee
     int32_t pass;                     // pass index within the cycle
     int32_t npass;                    // passes per cycle
-    int32_t write_eos;                // materialise p, c, g of the real cells on every pass (else on the last)
+    int32_t write_eos;                // p, c, g of the real cells: 1 on every pass, 0 on the last pass of a
+                                      // cycle, -1 never (the solver computes them when they are read)
     int32_t reuse;                    // reuse a predecessor's results over runs of identical inputs (exact)
     T gamma;
     T* buf[2][4];                     // two state sets: rho, umat, vmat, Emat
@@ -212,6 +213,12 @@ struct SweepArgs {
 // hold (the same single evaluation).  Loads and stores still happen for every cell.
 __device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
 __device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+
+// Whether a pass stores p, c, g of the cells it owns (SweepArgs::write_eos).
+template <bool LAST, class A_t> __device__ __forceinline__ bool writes_eos(const A_t& A)
+{
+    return A.write_eos > 0 || (LAST && A.write_eos == 0);
+}
 
 // rc = rho c, rcu = rc ua, dm = rho dx: the products that the two faces of a cell both use
 template <class T> struct CellIn { T rho, ua, uo, E, p, c, rc, rcu, dm; };
@@ -755,7 +762,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
             u.rho = run_slot[0][tid]; u.ua = run_slot[1][tid]; u.uo = run_slot[2][tid]; u.E = run_slot[3][tid];
             const T up = run_slot[4][tid], uc = run_slot[5][tid];
             const T u_out[4] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid], run_slot[9][tid]};
-            const bool pcg_out = LAST || A.write_eos;
+            const bool pcg_out = writes_eos<LAST>(A);
             const T g_out = (1 + A.gamma) / 2;
             // Along a row (s == 1) the cells of a batch are consecutive in memory: when every array's
             // address of the batch's first cell (and of its first result) is aligned to two values, the
@@ -959,7 +966,7 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                     c.dm = mul_dx(c.rho, g);
                 } else {
                     prepare(c);
-                    if (m == t && t >= a0 && t < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
+                    if (m == t && t >= a0 && t < b0 && writes_eos<LAST>(A)) {   // owned real cell: what update_EOS stores
                         A.pmat[idx] = c.p;
                         A.cmat[idx] = c.c;
                         A.gmat[idx] = (1 + A.gamma) / 2;

@@ -162,7 +162,7 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
             if (kGAD) { D2 = gad_diff<T, ADDS>(G2, c, c); D1 = D2; D0 = D2; }
         };
         const auto pcg = [&](int tt, const CellIn<T>& c) {
-            if (tt >= a0 && tt < b0 && (LAST || A.write_eos)) {   // owned real cell: what update_EOS stores
+            if (tt >= a0 && tt < b0 && writes_eos<LAST>(A)) {   // owned real cell: what update_EOS stores
                 const int64_t idx = base + (int64_t)tt * g.s;
                 A.pmat[idx] = c.p;
                 A.cmat[idx] = c.c;
@@ -195,7 +195,7 @@ __device__ __forceinline__ void sweep_faces(const SweepArgs<T>& A, const int blk
         const auto stream = [&](int t) -> int {
             const CellIn<T> u = run_cell();
             const T u_out[3] = {run_slot[6][tid], run_slot[7][tid], run_slot[8][tid]};
-            const bool pcg_out = LAST || A.write_eos;
+            const bool pcg_out = writes_eos<LAST>(A);
             while (t <= t1) {
                 const int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];

@@ -85,9 +85,15 @@ typedef struct armon_solver_opts {
     int32_t cycles_per_graph; /* cycles captured per CUDA graph launch (0 = default, 16) */
     int32_t seg_len;          /* cells per thread along the sweep axis (0 = automatic) */
     int32_t block_lines;      /* lines (threads) per block (0 = automatic, 128) */
-    int32_t materialize_eos;  /* write p, c, g of the real cells on every pass (1) or only on the
-                                 last pass of a cycle (0, default): the arrays the time loop leaves
-                                 are the same, since every pass's EOS overwrites the previous one */
+    int32_t materialize_eos;  /* p, c, g of the real cells: written by every pass (1), by the last
+                                 pass of each cycle (0), or (-1, default) computed from the last
+                                 pass's input, which the other state set still holds, when the loop
+                                 ends, when p, c or g is downloaded, uploaded or its device pointer
+                                 taken, or at the next begin_loop.  The values are the same in every
+                                 mode (each pass's EOS overwrites the previous one); with -1 the
+                                 arrays hold older values while cycles are still being issued
+                                 (armon_solver_enqueue_cycles).  Split passes write them on the last
+                                 pass in modes -1 and 0 (their cell half reads c). */
     int32_t unit_order;       /* 0 (default): each pass launches its blocks longest first, by the time
                                  each took in the previous cycle (results do not depend on it);
                                  -1: in index order */

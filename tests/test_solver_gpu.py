@@ -71,9 +71,10 @@ EXTRA = [
 
 
 @pytest.mark.parametrize("case", EXTRA, ids=lambda c: f"{c.test}-{c.scheme}-{c.projection}-{c.nx}x{c.ny}")
-@pytest.mark.parametrize("seg_len,graph,eos_every_pass", [(0, 16, 0), (16, 0, 1), (23, 3, 0)])
+@pytest.mark.parametrize("seg_len,graph,eos_every_pass", [(0, 16, -1), (16, 0, 1), (23, 3, 0), (40, 0, -1)])
 def test_fused_solver_matches_oracle_bitwise(case, seg_len, graph, eos_every_pass):
-    # p, c, g written on every pass or on the last pass of each cycle: the same final arrays
+    # p, c, g written on every pass, on the last pass of each cycle, or computed from the last pass's
+    # input when they are read: the same final arrays
     po, ref = _oracle_fields(case)
     s, p, status = run_solver(case, seg_len=seg_len, cycles_per_graph=graph, materialize_eos=eos_every_pass)
     with s:
@@ -284,3 +285,27 @@ def test_split_pass_gives_the_fused_bits(kw, precision):
     assert ta == tb and da == db
     for k in FIELDS:
         assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_eos_computed_when_read_matches_eos_written_by_the_passes(precision):
+    # materialize_eos -1 (default): p, c, g are computed from the last pass's input when they are
+    # downloaded or their device pointer taken, between cycles issued with enqueue_cycles, and give
+    # what the passes write in mode 0 (last pass of each cycle), cycle count after cycle count
+    case = A.Case(test="Sod_circ", scheme="GAD", projection="euler_2nd", nghost=5, nx=160, ny=96, cfl=0.6,
+                  max_cycles=40, max_time=1e9, test_option=0.04)
+    got = {}
+    for mode in (-1, 0):
+        with A.Solver(case, precision=precision, split_pass=-1, materialize_eos=mode) as s:
+            s.init_test()
+            out = []
+            for n in (3, 8, 12):
+                s.enqueue_cycles(n)
+                out.append({k: s.download(k) for k in ("pmat", "cmat", "gmat", "rho")})
+                if precision == 64:
+                    ptr = A.lib().armon_solver_device_array(s._h, A.ARRAYS.index("cmat"))
+                    assert ptr
+            got[mode] = out
+    for a, b in zip(got[-1], got[0]):
+        for k in a:
+            assert np.array_equal(a[k].view(np.int64), b[k].view(np.int64)), k

@@ -797,26 +797,33 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                     const int tw = __shfl_sync(full, t, 0);
                     if (!__all_sync(full, t == tw && t >= a0 && t + 32 <= b0 && t - H >= a0)) break;
                     int k_mine = 32;
+                    constexpr int kRows = 8;     // rows whose loads are in flight together
 #pragma unroll 1
-                    for (int r = 0; r < 32; r++) {
-                        const int sl = wbase + r;
-                        const int64_t rb = __shfl_sync(full, base, r);
-                        CellIn<T> ur;
-                        ur.rho = run_slot[0][sl]; ur.ua = run_slot[1][sl]; ur.uo = run_slot[2][sl]; ur.E = run_slot[3][sl];
-                        const int64_t idx = rb + tw + lane;
-                        CellIn<T> c;
-                        c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
-                        const unsigned bal = __ballot_sync(full, same_state(c, ur));
-                        const int kr = bal == full ? 32 : __ffs(~bal) - 1;
-                        if (lane < kr) {
-                            if (pcg_out) { A.pmat[idx] = run_slot[4][sl]; A.cmat[idx] = run_slot[5][sl]; A.gmat[idx] = g_out; }
-                            const int64_t o = idx - H;
-                            out[0][o] = run_slot[6][sl];
-                            out[axis == 0 ? 1 : 2][o] = run_slot[7][sl];
-                            out[axis == 0 ? 2 : 1][o] = run_slot[8][sl];
-                            out[3][o] = run_slot[9][sl];
+                    for (int r0 = 0; r0 < 32; r0 += kRows) {
+                        int64_t idx[kRows];
+                        CellIn<T> c[kRows];
+#pragma unroll
+                        for (int q = 0; q < kRows; q++) {
+                            idx[q] = __shfl_sync(full, base, r0 + q) + tw + lane;
+                            c[q].rho = rho_in[idx[q]]; c[q].ua = ua_in[idx[q]]; c[q].uo = uo_in[idx[q]]; c[q].E = E_in[idx[q]];
                         }
-                        if (lane == r) k_mine = kr;
+#pragma unroll
+                        for (int q = 0; q < kRows; q++) {
+                            const int sl = wbase + r0 + q;
+                            CellIn<T> ur;
+                            ur.rho = run_slot[0][sl]; ur.ua = run_slot[1][sl]; ur.uo = run_slot[2][sl]; ur.E = run_slot[3][sl];
+                            const unsigned bal = __ballot_sync(full, same_state(c[q], ur));
+                            const int kr = bal == full ? 32 : __ffs(~bal) - 1;
+                            if (lane < kr) {
+                                if (pcg_out) { A.pmat[idx[q]] = run_slot[4][sl]; A.cmat[idx[q]] = run_slot[5][sl]; A.gmat[idx[q]] = g_out; }
+                                const int64_t o = idx[q] - H;
+                                out[0][o] = run_slot[6][sl];
+                                out[axis == 0 ? 1 : 2][o] = run_slot[7][sl];
+                                out[axis == 0 ? 2 : 1][o] = run_slot[8][sl];
+                                out[3][o] = run_slot[9][sl];
+                            }
+                            if (lane == r0 + q) k_mine = kr;
+                        }
                     }
                     if (LAST && !counted && k_mine > 0) { add_dt(u_out, uc); counted = true; }
                     t += k_mine;

@@ -129,11 +129,6 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 #ifndef ARMON_REUSE_PREFETCH
 #define ARMON_REUSE_PREFETCH 0
 #endif
-// Whether a warp whose 32 threads stream their rows in step takes 32 positions of each row at a
-// time together (X pass of the fused march; 1 = on).
-#ifndef ARMON_REUSE_TILE
-#define ARMON_REUSE_TILE 1
-#endif
 template <class T> __host__ __device__ constexpr int reuse_batch() { return sizeof(T) == 8 ? ARMON_REUSE_BATCH : ARMON_REUSE_BATCH_F32; }
 constexpr int kReusePrefetch = ARMON_REUSE_PREFETCH;
 
@@ -783,53 +778,6 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 if (pcg_out) a |= (uintptr_t)(A.pmat + i) | (uintptr_t)(A.cmat + i) | (uintptr_t)(A.gmat + i);
                 return (a & mask) == 0;
             };
-            // Rows streamed by the whole warp (X pass): when all 32 threads stream at the same
-            // position with 32 owned positions ahead, each of the warp's 32 rows is read 32
-            // consecutive cells at a time (one line per access instead of one row per thread), each
-            // thread comparing its cell with that row's run state (the row owner's slot of shared
-            // memory) and storing its result; a ballot gives where each row's run ends.  Every
-            // decision to go on is a warp vote, so the warp stays together until it stops.
-            if (ARMON_REUSE_TILE && s == 1 && __activemask() == 0xffffffffu) {
-                const unsigned full = 0xffffffffu;
-                const int lane = tid & 31, wbase = tid & ~31;
-                __syncwarp(full);                // every thread's slot written (keep_run) before any is read
-                for (;;) {
-                    const int tw = __shfl_sync(full, t, 0);
-                    if (!__all_sync(full, t == tw && t >= a0 && t + 32 <= b0 && t - H >= a0)) break;
-                    int k_mine = 32;
-                    constexpr int kRows = 8;     // rows whose loads are in flight together
-#pragma unroll 1
-                    for (int r0 = 0; r0 < 32; r0 += kRows) {
-                        int64_t idx[kRows];
-                        CellIn<T> c[kRows];
-#pragma unroll
-                        for (int q = 0; q < kRows; q++) {
-                            idx[q] = __shfl_sync(full, base, r0 + q) + tw + lane;
-                            c[q].rho = rho_in[idx[q]]; c[q].ua = ua_in[idx[q]]; c[q].uo = uo_in[idx[q]]; c[q].E = E_in[idx[q]];
-                        }
-#pragma unroll
-                        for (int q = 0; q < kRows; q++) {
-                            const int sl = wbase + r0 + q;
-                            CellIn<T> ur;
-                            ur.rho = run_slot[0][sl]; ur.ua = run_slot[1][sl]; ur.uo = run_slot[2][sl]; ur.E = run_slot[3][sl];
-                            const unsigned bal = __ballot_sync(full, same_state(c[q], ur));
-                            const int kr = bal == full ? 32 : __ffs(~bal) - 1;
-                            if (lane < kr) {
-                                if (pcg_out) { A.pmat[idx[q]] = run_slot[4][sl]; A.cmat[idx[q]] = run_slot[5][sl]; A.gmat[idx[q]] = g_out; }
-                                const int64_t o = idx[q] - H;
-                                out[0][o] = run_slot[6][sl];
-                                out[axis == 0 ? 1 : 2][o] = run_slot[7][sl];
-                                out[axis == 0 ? 2 : 1][o] = run_slot[8][sl];
-                                out[3][o] = run_slot[9][sl];
-                            }
-                            if (lane == r0 + q) k_mine = kr;
-                        }
-                    }
-                    if (LAST && !counted && k_mine > 0) { add_dt(u_out, uc); counted = true; }
-                    t += k_mine;
-                    if (__ballot_sync(full, k_mine == 32) != full) break;
-                }
-            }
             while (t <= t1) {
                 int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];

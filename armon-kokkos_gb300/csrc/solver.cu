@@ -66,6 +66,7 @@ struct armon_solver {
         std::array<int, 9> key{};
     } tune;
     int64_t issued = 0;             // cycles issued since begin_loop
+    int64_t cycle0 = 0;             // the cycle count at begin_loop
     bool eos_stale = false;         // p, c, g of the last pass's input are not in memory yet
     double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
     bool ordered = true;            // longest-first dispatch of each pass's units
@@ -437,7 +438,7 @@ int finish_tuning(armon_solver* s)
     int rc = sync_state(s);
     if (rc != ARMON_OK) return rc;
     const StepState& st = *s->h_state;
-    const bool ran = st.status == STATUS_RUNNING && st.cycle == s->issued;
+    const bool ran = st.status == STATUS_RUNNING && st.cycle == s->cycle0 + s->issued;
     size_t best = 0;
     float best_t = 0.f;
     bool have = false;
@@ -694,6 +695,7 @@ int armon_solver_begin_loop(armon_solver* s)
     s->eos_stale = false;
     s->issued = 0;
     int rc = sync_state(s);
+    s->cycle0 = s->h_state->cycle;
     if (rc == ARMON_OK) rc = start_tuning(s);
     return rc;
 }

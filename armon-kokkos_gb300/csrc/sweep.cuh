@@ -117,19 +117,30 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 // Positions a run streams per iteration (loads issued together, then compared and stored), FP64
 // and FP32, and how many batches ahead the streaming loop asks L2 for the lines it will load next
 // (prefetch.global.L2: no registers, no data returned; 0 = none).  Measured at 4096² FP64 / 8192²
-// FP32, cycles 180-200 / 80-100 (G cell-updates/s): no prefetch 6.78 / 13.84, one batch ahead
-// 6.47 / 12.77, two 5.85 / 10.32; FP32 batches of 8: 12.72 (one ahead); FP64 batches of 8 or 16
-// (no prefetch): 6.41, 6.15.
+// FP32, cycles 180-200 / 80-100 (G cell-updates/s), with the general streaming loop: no prefetch
+// 6.78 / 13.84, one batch ahead 6.47 / 12.77, two 5.85 / 10.32; FP32 batches of 8: 12.72 (one
+// ahead); FP64 batches of 8 or 16 (no prefetch): 6.41, 6.15.  With the straight-line path and
+// pair accesses, FP32 batches of 8 against 4: 24.88 against 24.26-24.31 and 24.00 against
+// 23.78-23.80 (two runs), the X pass holding four pair loads per array in flight instead of two.
 #ifndef ARMON_REUSE_BATCH
 #define ARMON_REUSE_BATCH 4
 #endif
 #ifndef ARMON_REUSE_BATCH_F32
-#define ARMON_REUSE_BATCH_F32 4
+#define ARMON_REUSE_BATCH_F32 8
 #endif
 #ifndef ARMON_REUSE_PREFETCH
 #define ARMON_REUSE_PREFETCH 0
 #endif
+// Whether the straight-line streaming path takes the following batches in a loop of its own, with
+// the pair alignment of the run's positions taken once (bit 0 FP64, bit 1 FP32), instead of one
+// batch per iteration of the general loop, each testing its alignment.  FP32 gains 1.3 % from it
+// (25.35 against 25.03 G at 8192²); FP64 loses 6.5 % (7.00 against 7.49 G at 4096²), and 1 % with
+// the alignment alone taken once (7.38-7.43 against 7.49-7.55 G).
+#ifndef ARMON_REUSE_INNER
+#define ARMON_REUSE_INNER 2
+#endif
 template <class T> __host__ __device__ constexpr int reuse_batch() { return sizeof(T) == 8 ? ARMON_REUSE_BATCH : ARMON_REUSE_BATCH_F32; }
+template <class T> __host__ __device__ constexpr bool reuse_inner() { return ((ARMON_REUSE_INNER >> (sizeof(T) == 4 ? 1 : 0)) & 1) != 0; }
 constexpr int kReusePrefetch = ARMON_REUSE_PREFETCH;
 
 // Two consecutive values with one 8-byte (float) or 16-byte (double) access; p must be aligned to
@@ -778,43 +789,63 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                 if (pcg_out) a |= (uintptr_t)(A.pmat + i) | (uintptr_t)(A.cmat + i) | (uintptr_t)(A.gmat + i);
                 return (a & mask) == 0;
             };
+            // every address moves by two values from position tt to tt + 2, so the alignment of a
+            // position is that of the first or the second position of the run, by parity (taken
+            // once with reuse_inner; the FP64 pass measured faster testing each batch)
+            const int ts = t;
+            const bool hoist = reuse_inner<T>() && s == 1 && kReuseBatch % 2 == 0;
+            const bool even_aligned = hoist && pair_aligned(ts);
+            const bool odd_aligned = hoist && pair_aligned(ts + 1);
             while (t <= t1) {
                 int nb = min(kReuseBatch, t1 - t + 1);
                 bool same[kReuseBatch];
                 bool fast = nb == kReuseBatch && t >= a0 && t + kReuseBatch <= b0 && t - H >= a0;
                 bool pairs = false;
                 if (fast && s == 1 && kReuseBatch % 2 == 0) {
-                    pairs = pair_aligned(t);
-                    if (!pairs && pair_aligned(t + 1)) { fast = false; nb = 1; }   // one position to the alignment
+                    bool next;   // whether the next position is aligned
+                    if (reuse_inner<T>()) {
+                        const bool odd = ((t - ts) & 1) != 0;
+                        pairs = odd ? odd_aligned : even_aligned;
+                        next = odd ? even_aligned : odd_aligned;
+                    } else {
+                        pairs = pair_aligned(t);
+                        next = !pairs && pair_aligned(t + 1);
+                    }
+                    if (!pairs && next) { fast = false; nb = 1; }   // one position to the alignment
                 }
                 if (fast) {
-                    // a batch of real cells the segment owns, each with a result to store: no mirror,
-                    // no ghost, and the stores need no per-position test
-                    if (pairs) {
+                    // batches of real cells the segment owns, each with a result to store: no mirror,
+                    // no ghost, and the stores need no per-position test.  Every batch up to tf is
+                    // such a batch, with the same alignment (the batch is an even number of cells);
+                    // with reuse_inner they are taken here, else one per iteration of the loop.
+                    const int tf = min(b0, t1 + 1) - kReuseBatch;
+                    bool all;
+                    for (;;) {
+                        if (pairs) {
 #pragma unroll
-                        for (int q = 0; q < kReuseBatch; q += 2) {
-                            const int64_t idx = base + t + q;
-                            CellIn<T> c0, c1;
-                            load2(rho_in + idx, c0.rho, c1.rho);
-                            load2(ua_in + idx, c0.ua, c1.ua);
-                            load2(uo_in + idx, c0.uo, c1.uo);
-                            load2(E_in + idx, c0.E, c1.E);
-                            same[q] = same_state(c0, u);
-                            same[q + 1] = same_state(c1, u);
+                            for (int q = 0; q < kReuseBatch; q += 2) {
+                                const int64_t idx = base + t + q;
+                                CellIn<T> c0, c1;
+                                load2(rho_in + idx, c0.rho, c1.rho);
+                                load2(ua_in + idx, c0.ua, c1.ua);
+                                load2(uo_in + idx, c0.uo, c1.uo);
+                                load2(E_in + idx, c0.E, c1.E);
+                                same[q] = same_state(c0, u);
+                                same[q + 1] = same_state(c1, u);
+                            }
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < kReuseBatch; q++) {
+                                const int64_t idx = base + (int64_t)(t + q) * s;
+                                CellIn<T> c;
+                                c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
+                                same[q] = same_state(c, u);
+                            }
                         }
-                    } else {
+                        all = true;
 #pragma unroll
-                        for (int q = 0; q < kReuseBatch; q++) {
-                            const int64_t idx = base + (int64_t)(t + q) * s;
-                            CellIn<T> c;
-                            c.rho = rho_in[idx]; c.ua = ua_in[idx]; c.uo = uo_in[idx]; c.E = E_in[idx];
-                            same[q] = same_state(c, u);
-                        }
-                    }
-                    bool all = true;
-#pragma unroll
-                    for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
-                    if (all) {
+                        for (int q = 0; q < kReuseBatch; q++) all = all && same[q];
+                        if (!all) break;     // same[] of this batch: the positions up to the first that differs are stored below
                         if (pairs) {
 #pragma unroll
                             for (int q = 0; q < kReuseBatch; q += 2) {
@@ -839,8 +870,9 @@ __device__ __forceinline__ void sweep_domain(const SweepArgs<T>& A, const int bl
                         }
                         if (LAST && !counted) { add_dt(u_out, uc); counted = true; }
                         t += kReuseBatch;
-                        continue;
+                        if (!reuse_inner<T>() || t > tf) break;
                     }
+                    if (all) continue;       // past tf (or one batch taken): the general loop goes on
                 } else {
 #pragma unroll
                     for (int q = 0; q < kReuseBatch; q++) {

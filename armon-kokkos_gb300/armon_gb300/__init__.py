@@ -135,6 +135,8 @@ def lib() -> C.CDLL:
     L.armon_solver_tiling.argtypes = [S, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.armon_solver_block_lines.argtypes = [S]
     L.armon_solver_tuning.argtypes = [S]
+    L.armon_solver_measurement_cycles.argtypes = [S]
+    L.armon_solver_measurement_cycles.restype = C.c_int64
     L.armon_solver_split_pass.argtypes = [S]
     L.armon_tiling_cache_clear.argtypes = []
     L.armon_tiling_cache_clear.restype = None
@@ -326,6 +328,10 @@ class Solver:
     def tuning(self) -> bool:
         """True while the time loop is still timing candidate tilings on its cycles."""
         return lib().armon_solver_tuning(self._h) == 1
+
+    def measurement_cycles(self) -> int:
+        """Cycles run so far with a candidate tiling of the tiling measurement."""
+        return int(lib().armon_solver_measurement_cycles(self._h))
 
     def split_pass(self) -> bool:
         """True when the axis passes run split (face launch + cell launch), False when fused."""

@@ -67,6 +67,7 @@ struct armon_solver {
     } tune;
     int64_t issued = 0;             // cycles issued since begin_loop
     int64_t cycle0 = 0;             // the cycle count at begin_loop
+    int64_t measure_cycles = 0;     // cycles run with a candidate tiling, over the solver's loops
     bool eos_stale = false;         // p, c, g of the last pass's input are not in memory yet
     double* stage = nullptr;        // FP32 solvers: FP64 staging array for uploads and downloads
     bool ordered = true;            // longest-first dispatch of each pass's units
@@ -464,7 +465,7 @@ int enqueue(armon_solver* s, int n_cycles)
     auto& T = s->tune;
     while (n_cycles > 0 && T.active) {
         int rc = ARMON_OK;
-        if (s->issued + 1 > s->cfg.max_cycles) {   // the loop ends first: keep the model's tiling
+        if (s->cycle0 + s->issued + 1 > s->cfg.max_cycles) {   // the loop ends first: keep the model's tiling
             end_tuning(s);
             rc = apply_tiling(s, model_tiling(s));
             if (rc != ARMON_OK) return rc;
@@ -478,7 +479,9 @@ int enqueue(armon_solver* s, int n_cycles)
             rc = apply_tiling(s, T.cand[T.seq[T.pos]]);
             if (rc == ARMON_OK) rc = enqueue_direct(s, 1);
             T.warm = false;
+            s->measure_cycles++;
         } else {
+            s->measure_cycles++;
             CUDA_TRY(cudaEventRecord(T.ev[2 * T.pos], s->stream));
             rc = enqueue_direct(s, 1);
             if (rc == ARMON_OK) CUDA_TRY(cudaEventRecord(T.ev[2 * T.pos + 1], s->stream));
@@ -881,6 +884,8 @@ int armon_solver_tiling(armon_solver* s, int32_t seg_len[2], int32_t blocks[2])
 int armon_solver_block_lines(const armon_solver* s) { return s->block; }
 
 int armon_solver_tuning(const armon_solver* s) { return s->tune.active ? 1 : 0; }
+
+int64_t armon_solver_measurement_cycles(const armon_solver* s) { return s->measure_cycles; }
 
 int armon_solver_split_pass(const armon_solver* s) { return s->split ? 1 : 0; }
 

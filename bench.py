@@ -340,6 +340,7 @@ def single_run(A, args, nx: int, prec: int, K: int, W: int, run_cycles: int, str
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = s.kernel_launches
+    measured0 = s.measurement_cycles()
 
     def timed():
         ev[1].record(stream)
@@ -352,12 +353,14 @@ def single_run(A, args, nx: int, prec: int, K: int, W: int, run_cycles: int, str
 
     ms, clocks = sampled(timed)
     launches = s.kernel_launches - launches0
+    measured_in_window = s.measurement_cycles() - measured0
     p, status = s.state()
     if status != 0 or p.cycle != total:
         raise RuntimeError(f"solver state after the timed region: status {status}, cycle {p.cycle}")
     tiling, blocks = s.tiling()
     return {"ms": ms, "total": total, "clocks": clocks, "launches": launches,
             "tiling": tiling, "blocks": blocks, "block_lines": s.block_lines(), "tuning_left": tuning_left,
+            "measured_in_window": measured_in_window, "measurement_cycles": s.measurement_cycles(),
             "split": s.split_pass(), "solver": s}
 
 
@@ -454,7 +457,9 @@ def run_gpu(args) -> None:
                "config": dict(config(nx, nx, world, prec, r["total"]), seg_len=list(r["tiling"]),
                               blocks=list(r["blocks"]), block_lines=r["block_lines"], split_pass=r["split"],
                               reuse=args.reuse == 0, timed_cycles=[r["total"] - K, r["total"]],
-                              tiling_measured_before_timing=not r["tuning_left"]),
+                              tiling_measured_before_timing=not r["tuning_left"],
+                              tiling_measurement_cycles=r["measurement_cycles"],
+                              tiling_measurement_cycles_timed=r["measured_in_window"]),
                "whole_run": {"value": whole, "unit": METRIC, "cycles": run_cycles,
                              "note": "every cycle of the whole run, from the initial state, on the device (CUDA events "
                                      "around begin_loop and the time loop of the e2e solve)"},
@@ -520,7 +525,9 @@ def fp32_line(A, args, stream) -> dict:
     cells = nx * nx
     return {"value": cells * K / (r["ms"] / 1e3), "unit": METRIC, "ms_per_step": r["ms"] / K, "steps": K, "warmup": W,
             "config": dict(config(nx, nx, 1, 32, r["total"]), seg_len=list(r["tiling"]), block_lines=r["block_lines"],
-                           split_pass=r["split"], timed_cycles=[r["total"] - K, r["total"]]),
+                           split_pass=r["split"], timed_cycles=[r["total"] - K, r["total"]],
+                           tiling_measurement_cycles=r["measurement_cycles"],
+                           tiling_measurement_cycles_timed=r["measured_in_window"]),
             "roofline": roofline(32, cells, r["ms"] / K, r["split"]),
             "accuracy": fp32_accuracy(A, nx, 100, args.graph) if args.accuracy_cycles > 0 else None,
             "gpu_launches": r["launches"], "clocks": r["clocks"]}

@@ -173,6 +173,9 @@ int armon_solver_block_lines(const armon_solver* s);
 /* 1 while the time loop is still measuring candidate tilings on its cycles (domains of 2^20 cells
  * or more whose geometry this process has not measured yet; results never depend on the tiling). */
 int armon_solver_tuning(const armon_solver* s);
+/* Cycles this solver has run with a candidate tiling of the tiling measurement so far (a cost cycle
+ * and a timed cycle per candidate and visit). */
+int64_t armon_solver_measurement_cycles(const armon_solver* s);
 /* 1 when the axis passes run split (a face launch and a cell launch), 0 when fused: the caller's
  * split_pass, or the measured form when split_pass is 0 and the solver holds a face buffer. */
 int armon_solver_split_pass(const armon_solver* s);

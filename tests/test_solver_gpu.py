@@ -231,15 +231,19 @@ def test_tiling_measured_on_the_loops_own_cycles(precision):
         s.run()
         p, status = s.state()
         assert status == 0 and p.cycle == 120 and not s.tuning()
+        assert s.measurement_cycles() > 0 and s.measurement_cycles() % 2 == 0
         got = ({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt)
     with A.Solver(case, precision=precision) as s:
         s.init_test()
         assert not s.tuning()           # the cached choice
+        s.run(cycle_limit=30)
+        assert s.measurement_cycles() == 0
     with A.Solver(case, precision=precision, seg_len=128) as s:
         s.init_test()
         assert not s.tuning()
         s.run()
         p, status = s.state()
+        assert s.measurement_cycles() == 0
         ref = ({k: s.download(k) for k in FIELDS}, p.time, p.current_cycle_dt)
     assert got[1:] == ref[1:]
     for k in FIELDS:

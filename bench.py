@@ -441,8 +441,8 @@ def run_gpu(args) -> None:
     value = whole_job_rate(cells * K, world, ms_max / 1e3)
     # end to end, from the run's initial state (init_test of a fresh solver) in pinned host memory,
     # the results into pinned buffers that the library has written once before, as those of an
-    # application that reuses them (the library's first copy into a new pinned buffer costs some
-    # 7 ms per 135 MB once, later ones 0.7 ms)
+    # application that reuses them (the first device-to-host copy into a newly allocated pinned block
+    # costs 5-7.5 ms per 135 MB once, later ones 0.73 ms)
     with A.Solver(A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": 1}), precision=prec) as s0:
         s0.init_test()
         ins = {k: torch.from_numpy(s0.download(k)).pin_memory() for k in ("rho", "umat", "vmat", "Emat")}

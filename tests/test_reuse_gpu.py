@@ -110,16 +110,23 @@ def test_reuse_matches_oracle(case):
             assert same_bits(got[k], ref[k]), (split_pass, k)
 
 
-def test_batch_reuse_is_bit_identical():
+@pytest.mark.parametrize("precision", [64, 32])
+def test_batch_reuse_is_bit_identical(precision):
+    # the batch kernels' streaming (FP32: batches of eight cells in a loop of their own) against every
+    # position computed, and each domain against its solo solver
     cases = [CASES[0], A.Case(**{**CASES[0].__dict__, "nx": 64, "ny": 300}),
              A.Case(**{**CASES[0].__dict__, "nx": 333, "ny": 41})]
     states = [runs_state(c, seed=k) for k, c in enumerate(cases)]
     results = {}
     for reuse in (-1, 0):
-        with A.Batch(cycles_per_graph=4, reuse=reuse) as b:
+        with A.Batch(precision=precision, cycles_per_graph=4, reuse=reuse) as b:
             ids = [b.add(A.make_params(c), st) for c, st in zip(cases, states)]
             assert b.run() == 0
             results[reuse] = [{k: A.real_cells(b.params[i], b.download(i, k)) for k in FIELDS} for i in ids]
     for a, r in zip(results[0], results[-1]):
         for k in FIELDS:
             assert same_bits(a[k], r[k]), k
+    for c, st, a in zip(cases, states, results[0]):
+        _, solo = solve(c, st, precision=precision)
+        for k in FIELDS:
+            assert same_bits(a[k], solo[k]), k

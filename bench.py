@@ -440,9 +440,8 @@ def run_gpu(args) -> None:
     ms_max = max_over_ranks(r["ms"], world)
     value = whole_job_rate(cells * K, world, ms_max / 1e3)
     # end to end, from the run's initial state (init_test of a fresh solver) in pinned host memory,
-    # the results into pinned buffers that the library has written once before, as those of an
-    # application that reuses them (the first device-to-host copy into a newly allocated pinned block
-    # costs 5-7.5 ms per 135 MB once, later ones 0.73 ms)
+    # the results into pinned buffers allocated and written once before, as those of an application
+    # that reuses them
     with A.Solver(A.Case(**{**WORKLOAD, "nx": nx, "ny": nx, "max_cycles": 1}), precision=prec) as s0:
         s0.init_test()
         ins = {k: torch.from_numpy(s0.download(k)).pin_memory() for k in ("rho", "umat", "vmat", "Emat")}
@@ -474,7 +473,7 @@ def run_gpu(args) -> None:
                        "h2d_bytes_per_step": 4 * nb * 8 / run_cycles, "d2h_bytes_per_step": 5 * nb * 8 / run_cycles,
                        "seconds": e2e_s, "host_arrays": "FP64 (converted to the solver's precision inside the call)",
                        "path": f"armon_solver_upload x4 (pinned) + begin_loop + {run_cycles} cycles + "
-                               "armon_solver_download x5 (into pinned buffers the library has written once "
+                               "armon_solver_download x5 (into pinned buffers allocated and written once "
                                "before); tiling already measured in this process"},
                "e2e_cold": {"value": cold_value, "unit": METRIC, "seconds": cold_s, "cycles": run_cycles,
                             "loop_value": cells * run_cycles / (cold_loop_ms / 1e3),

@@ -121,7 +121,8 @@ template <class T> __host__ __device__ constexpr bool sweep_prefetch() { return 
 // 6.78 / 13.84, one batch ahead 6.47 / 12.77, two 5.85 / 10.32; FP32 batches of 8: 12.72 (one
 // ahead); FP64 batches of 8 or 16 (no prefetch): 6.41, 6.15.  With the straight-line path and
 // pair accesses, FP32 batches of 8 against 4: 24.88 against 24.26-24.31 and 24.00 against
-// 23.78-23.80 (two runs), the X pass holding four pair loads per array in flight instead of two.
+// 23.78-23.80 (two runs), the X pass holding four pair loads per array in flight instead of two;
+// FP64 batches of 2, 6, 8 against 4: 7.51, 6.84, 6.84 against 7.54.
 #ifndef ARMON_REUSE_BATCH
 #define ARMON_REUSE_BATCH 4
 #endif
